@@ -1,0 +1,253 @@
+/* ard_gb300.h -- C ABI of the GB300 ARD time-step library (libard_gb300.so).
+ *
+ * The library replaces the per-step loop of pjx3/ARD-simulator,
+ * Simulation::Update (ARD-simulator-190113/simulation.cpp:300-318), with
+ * hand-written sm_103a CUDA kernels.  The reference's object model stays the
+ * host-side description: a scene is the flattened list of partitions
+ * (Partition / DctPartition / PmlPartition), boundaries (Boundary), sound
+ * sources (SoundSource) and recorders (Recorder), in the reference's own list
+ * order, because the order decides which interface wins where interface
+ * strips overlap (boundary.cpp:21-173 overwrites; one thread => last wins).
+ *
+ * All entry points are plain C: integers, floats, pointers and sizes.  Every
+ * call returns ARD_OK (0) or an ARD_ERR_* code; ard_last_error() gives the
+ * message.  The caller owns host buffers; a context owns its device memory.
+ * A context is used from one host thread at a time; contexts are independent.
+ * Cells are integers in units of dh; fields are float32, row-major [z][y][x]
+ * with x fastest, as in DctVolume (dct_volume.cpp:72) and PmlPartition
+ * (pml_partition.cpp:6-15).
+ */
+#ifndef ARD_GB300_H
+#define ARD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ARD_ABI_VERSION 1
+
+/* ---- status codes ---- */
+enum {
+  ARD_OK = 0,
+  ARD_ERR_INVALID = 1,   /* malformed scene or argument */
+  ARD_ERR_CUDA = 2,      /* CUDA runtime error (message has the CUDA name) */
+  ARD_ERR_OOM = 3,       /* device allocation failed */
+  ARD_ERR_STATE = 4,     /* call not valid in the context's current state */
+  ARD_ERR_UNSTABLE = 5,  /* non-finite recorder sample or dt over the PML CFL limit */
+  ARD_ERR_RANGE = 6,     /* index / time range outside what the context holds */
+  ARD_ERR_NOGPU = 7      /* no CUDA device, or the kernels were not built for it */
+};
+
+/* Partition kinds: DctPartition / PmlPartition. */
+enum { ARD_PART_DCT = 0, ARD_PART_PML = 1 };
+
+/* PmlPartition::PmlType, same order (pml_partition.h:39-46). */
+enum {
+  ARD_PML_LEFT = 0,
+  ARD_PML_RIGHT = 1,
+  ARD_PML_TOP = 2,
+  ARD_PML_BOTTOM = 3,
+  ARD_PML_FRONT = 4,
+  ARD_PML_BACK = 5
+};
+
+/* Boundary::BoundaryType, same order (boundary.h:30-34). */
+enum { ARD_BOUNDARY_X = 0, ARD_BOUNDARY_Y = 1, ARD_BOUNDARY_Z = 2 };
+
+/* One Partition (partition.h:13-74): cell origin and extent. */
+typedef struct ard_partition {
+  int32_t kind;      /* ARD_PART_DCT or ARD_PART_PML */
+  int32_t pml_type;  /* ARD_PML_* for PML partitions, -1 for DCT partitions */
+  int32_t x_start, y_start, z_start;
+  int32_t width, height, depth;
+} ard_partition;
+
+/* One Boundary (boundary.h:9-46): a_ and b_ are indices into the scene's
+ * partition list; the ranges are Boundary::x_start_ .. z_end_. */
+typedef struct ard_boundary {
+  int32_t type;  /* ARD_BOUNDARY_* */
+  int32_t a, b;
+  int32_t x_start, x_end, y_start, y_end, z_start, z_end;
+  float absorption;
+} ard_boundary;
+
+/* A sound source or recorder at a global cell.  partition is the air
+ * partition it belongs to: for sources the one whose half-open box holds the
+ * cell (simulation.cpp:37-48), for recorders the first one that passes
+ * Recorder::FindPartition's 5-cell margin test (recorder.cpp:26-38). */
+typedef struct ard_point {
+  int32_t x, y, z;
+  int32_t partition;
+} ard_point;
+
+/* A whole scene: the reference's Simulation after its constructor ran.
+ * partitions: air partitions first, then PMLs, as Simulation::m_partitions.
+ * boundaries: Simulation::m_boundaries order. */
+typedef struct ard_scene {
+  float dh;             /* Simulation::m_dh (m) */
+  float dt;             /* Simulation::m_dt (s) */
+  float c0;             /* Simulation::m_c0 (m/s) */
+  int32_t pml_layers;   /* Simulation::m_pml_layers */
+  float pml_R;          /* PmlPartition::R_ (pml_partition.h:8), 1e-5 */
+  float modal_damping;  /* DctPartition::Update's 0.999f (dct_partition.cpp:68) */
+  int32_t n_partitions;
+  const ard_partition* partitions;
+  int32_t n_boundaries;
+  const ard_boundary* boundaries;
+  int32_t n_sources;
+  const ard_point* sources;
+  int32_t n_recorders;
+  const ard_point* recorders;
+} ard_scene;
+
+/* ===================================================================== */
+/* Host-side scene construction (no GPU needed).                          */
+/* ===================================================================== */
+
+/* Parameters of a scene build; the reference keeps them as static members
+ * set in main.cpp:29-45. */
+typedef struct ard_scene_params {
+  float dh, dt, c0;
+  int32_t pml_layers;
+  float absorption;     /* Partition::m_absorption, used for PML interfaces */
+  float pml_R;          /* 0 selects 1e-5 */
+  float modal_damping;  /* 0 selects 0.999 */
+} ard_scene_params;
+
+typedef struct ard_scene_buf ard_scene_buf;
+
+/* Builds a scene from air partitions given as cell boxes (6 ints each:
+ * x, y, z, width, height, depth), exactly as Simulation::Simulation
+ * (simulation.cpp:14-294) does: pairwise Boundary::FindBoundary
+ * (boundary.cpp:289-334) with Partition::AddBoundary's free-border marking
+ * (partition.cpp:96-143), source attachment, then per air partition the
+ * left/right/top/bottom PML runs over z-slice 0 of the free-border maps and
+ * the always-present front and back PMLs, each with its interface.
+ * Recorders get their partition by Recorder::FindPartition.
+ * src_cells / rec_cells hold 3 ints (x, y, z) per point. */
+int ard_scene_build(const ard_scene_params* params,
+                    int32_t n_air, const int32_t* air_boxes,
+                    int32_t n_sources, const int32_t* src_cells,
+                    int32_t n_recorders, const int32_t* rec_cells,
+                    ard_scene_buf** out);
+
+/* Same, reading the reference's integer-metre text files (README.md:13-37;
+ * Partition::ImportPartitions partition.cpp:151-176,
+ * SoundSource::ImportSources sound_source.cpp:24-48,
+ * Recorder::ImportRecorders recorder.cpp:67-89): each value is divided by dh
+ * in float and truncated to int.  recorders_path may be NULL. */
+int ard_scene_import(const ard_scene_params* params,
+                     const char* partitions_path,
+                     const char* sources_path,
+                     const char* recorders_path,
+                     ard_scene_buf** out);
+
+/* The scene held by a buffer (valid until ard_scene_free). */
+const ard_scene* ard_scene_get(const ard_scene_buf* buf);
+void ard_scene_free(ard_scene_buf* buf);
+
+/* Message of the last failed scene build on this thread. */
+const char* ard_scene_last_error(void);
+
+/* GaussianSource::SampleValue (gaussian_source.cpp:16-20) for t = 0..n-1:
+ * 1e9 * exp(-(pi * (2 * (c0*dt/dh) * t / 6 - 2))^2), evaluated in float. */
+int ard_gaussian_series(float c0, float dt, float dh, int64_t n, float* out);
+
+/* ===================================================================== */
+/* GPU time stepping.                                                     */
+/* ===================================================================== */
+
+typedef struct ard_ctx ard_ctx;
+
+enum { ARD_PREC_F32 = 0, ARD_PREC_F64 = 1 };
+
+typedef struct ard_options {
+  int32_t precision;     /* ARD_PREC_F32 (product path) or ARD_PREC_F64 (GPU oracle) */
+  int64_t max_steps;     /* capacity of source series and recorder history */
+  int32_t use_graphs;    /* capture step sequences in CUDA graphs (default 1) */
+  int32_t device;        /* CUDA device ordinal */
+  int32_t autotune;      /* pick kernel tile shapes per extent by timing (default 0) */
+} ard_options;
+
+/* Creates a context holding n_scenes independent scenes.  n_scenes > 1 is the
+ * batched mode: every stage runs as one launch over all scenes' work tables.
+ * opt may be NULL (defaults: f32, max_steps 4096, graphs on, device 0). */
+int ard_create(const ard_scene* scenes, int32_t n_scenes,
+               const ard_options* opt, ard_ctx** out);
+int ard_destroy(ard_ctx* ctx);
+
+/* Time series injected by source `source` of scene `scene` (replaces the
+ * default all-zero series).  Sample t is written into the force cell at step
+ * t, as Partition::ComputeSourceForcingTerms (partition.cpp:187-197) does
+ * with SoundSource::SampleValue(t).  n <= max_steps. */
+int ard_set_source_series(ard_ctx* ctx, int32_t scene, int32_t source,
+                          const float* series, int64_t n);
+
+/* Initial pressure of air partition `partition` (width*height*depth floats,
+ * [z][y][x]).  Sets both modal time levels so that the partition starts at
+ * rest with this pressure.  Only before the first step (or after reset). */
+int ard_set_initial_pressure(ard_ctx* ctx, int32_t scene, int32_t partition,
+                             const float* pressure);
+
+/* Per-face multipliers of the PML damping profile zeta (pml_partition.cpp:
+ * 69-86), indexed by ARD_PML_*.  Default all 1. */
+int ard_set_pml_scale(ard_ctx* ctx, int32_t scene, const float scale[6]);
+
+/* Zeroes all state and sets the step counter to 0 (series and scales stay). */
+int ard_reset(ard_ctx* ctx);
+
+/* Advances every scene by nsteps steps on `stream` (a cudaStream_t; NULL
+ * means the context's own stream).  Stream-ordered: returns once the work is
+ * queued.  Each step is Simulation::Update's phase A (source forcing, air
+ * partition modal update, PML update) then phase B (interface forcing). */
+int ard_step(ard_ctx* ctx, int64_t nsteps, void* stream);
+
+/* Waits for all work queued on the context's streams. */
+int ard_synchronize(ard_ctx* ctx);
+
+/* Current step counter (number of steps taken since create/reset). */
+int ard_time_step(const ard_ctx* ctx, int64_t* out);
+
+/* Recorder samples of scene `scene` for steps t0 .. t0+nt-1, written as
+ * out[t][recorder] (n_recorders floats per step).  The sample of step t is
+ * the pressure after step t's update, as Recorder::RecordField
+ * (recorder.cpp:40-57) takes it after Simulation::Update.  Synchronous. */
+int ard_read_recorders(ard_ctx* ctx, int32_t scene, float* out, int64_t t0, int64_t nt);
+
+/* Current pressure field of partition `partition` of scene `scene`
+ * (width*height*depth floats, [z][y][x]).  Synchronous.  For an air
+ * partition this runs the full inverse transform of the current modes. */
+int ard_read_field(ard_ctx* ctx, int32_t scene, int32_t partition, float* out);
+
+/* ---- adjoint (gradients of a recorder misfit) ---- */
+
+/* Gradients of J = 0.5 * sum_{t<T} sum_r w_r (rec[t][r] - target[t][r])^2
+ * over the first T steps of every scene, computed by the hand-written adjoint
+ * kernels with checkpoints of the two modal time levels (and PML state)
+ * every `checkpoint_every` steps and recomputation in between.  The forward
+ * run is done inside this call from the current initial state (reset first).
+ * target: T * n_recorders floats per scene, concatenated over scenes.
+ * Outputs (any may be NULL), concatenated over scenes:
+ *   grad_source  T * n_sources floats per scene    dJ/d(source series)
+ *   grad_scale   6 floats per scene                dJ/d(PML face scale)
+ *   loss         1 float per scene
+ * grad_initial_pressure is read back per partition with
+ * ard_read_initial_pressure_grad. */
+int ard_adjoint(ard_ctx* ctx, int64_t T, const float* target,
+                int32_t checkpoint_every,
+                float* grad_source, float* grad_scale, float* loss);
+int ard_read_initial_pressure_grad(ard_ctx* ctx, int32_t scene, int32_t partition,
+                                   float* out);
+
+/* Message of the last error on this context (NULL ctx: last create error). */
+int ard_last_error(const ard_ctx* ctx, char* buf, int64_t n);
+
+/* Library version / ABI check. */
+int ard_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ARD_GB300_H */
