@@ -1,0 +1,117 @@
+// Device-side work tables of the GB300 ARD engine.
+//
+// Memory layout in HBM (one allocation per element type; every table entry
+// holds element offsets into it):
+//
+//   air partition (w x h x d cells, N = w*h*d)
+//     M[2][N]        modal amplitudes, two time levels, [kz][ky][kx]
+//     cwt[N], psi[N] cos(w dt) and 2(1-cos(w dt))/w^2, built in FP64
+//     f{X,Y,Z}       force on the 3-cell shell: X layers [6][d][h] own the
+//                    cells with x in {0,1,2,w-3,w-2,w-1}; Y layers [6][d][w]
+//                    own y in {0,1,2,h-3,h-2,h-1} with x inside; Z layers
+//                    [6][h][w] own z in {0,1,2,d-3,d-2,d-1} with x, y inside
+//     p{X,Y,Z}       pressure on the same face layers, each layer complete
+//     P{X,Y,Z}       2D DCT-II of the force layers, combined as
+//                    layer(n) +/- layer(5-n): [2][3][..]
+//     R{X,Y,Z}       mode-space contractions onto the face rows, per tile
+//                    partial: [nb][2][3][..]
+//     tmp{X,Y,Z}     transform scratch [6][..]
+//   PML slab (L layers along its normal, plane A x B, B fastest)
+//     p[2], phi_n[2], phi_a[2], phi_b[2]   [L][A][B]
+//     force strip    [3][A][B] (the 3 layers next to the air partition)
+//
+// The modal update of an air partition needs the force only on the shell and
+// yields pressure only where the interfaces (shell) and recorders read it, so
+// the dense 3D DCT pair of the reference (dct_partition.cpp:48-73) becomes:
+// 2D transforms of 18 face layers, one fused pass over the modes
+// (expansion of the face transforms along the third axis + modal update +
+// contraction onto the face rows), and 2D inverse transforms of the face
+// layers.  DCT-II basis C_n(k, j) = 2 cos(pi (j + 1/2) k / n) throughout;
+// C_n(k, n-1-j) = (-1)^k C_n(k, j) pairs layer j with layer 5-j.
+#pragma once
+
+#include <cstdint>
+
+namespace ard {
+
+constexpr int kMaxPointsPerPart = 8;  // sources or recorders per air partition per modal tile
+constexpr int kModalTY = 4;           // ky rows per warp tile of the modal kernel
+
+struct DctDev {
+  int w, h, d;
+  int nbx, nby, nbz, TZ;  // modal tiling: 32-wide kx chunks, TY ky rows, TZ kz planes
+  int tile0;              // index of this partition's first modal tile
+  int src0, nsrc;         // attached sources (into PointDev table)
+  int rec0, nrec;         // attached recorders
+  long long M[2];
+  long long cwt, psi;
+  long long fX, fY, fZ;
+  long long pX, pY, pZ;
+  long long PX, PY, PZ;
+  long long RX, RY, RZ;
+  long long tmpX, tmpY, tmpZ;
+  long long cw, ch, cd;   // cosine tables C[k][j] (n*n) of extents w, h, d
+  long long recpart;      // [ntiles][nrec] recorder partial sums
+  double sf;              // forward scale 1 / (2 sqrt(2N))
+  double si8;             // inverse scale / 8: 1 / (8 sqrt(2N))
+  double damping;
+};
+
+struct PointDev {
+  int part;     // air partition (engine index)
+  int x, y, z;  // local cell
+  int slot;     // global source / recorder index
+};
+
+struct PmlDev {
+  int type;               // ARD_PML_*
+  int L, A, B;            // layers along the normal; plane A x B (B fastest)
+  int strip0;             // first layer of the forced strip (L-3 or 0)
+  int scene;
+  long long p[2];
+  long long phn[2], pha[2], phb[2];
+  long long force;        // [3][A][B]
+  long long zeta;         // [L] damping profile (scaled)
+  long long n;            // L*A*B
+};
+
+// Side of an interface: an air partition's face layers or a PML slab, both
+// seen as [layer][v][u] arrays in the face's (u fast, v slow) coordinates.
+struct SideDev {
+  int kind;     // 0 air, 1 PML
+  int idx;      // engine index (DctDev or PmlDev)
+  int ou, ov;   // global (u, v) of the side's origin
+  int ext;      // extent along the crossing axis
+  int self;     // include_self_terms_
+};
+
+struct IfaceDev {
+  int type;               // ARD_BOUNDARY_X/Y/Z: crossing axis
+  int u0, u1, v0, v1;     // global face range
+  SideDev lo, hi;         // left/top/front and right/bottom/back
+  double absorption;
+  long long mask;         // [cells] 6-bit write masks (bit m+3)
+  long long cell0;        // first global face-cell index of this interface
+};
+
+// One batched 1D transform job over lines of a 2D array.
+//   rows mode: lines are contiguous rows, array [batch][n]
+//   cols mode: lines are columns, array [n][batch]
+// Input = sum over `nparts` partial slabs (stride part_stride) of
+// in0 + sgn * in1 (in1 < 0: absent).  Forward: out_k = scale sum_j C[k][j] x_j;
+// inverse: out_j = scale sum_k C[k][j] x_k.
+struct XformJob {
+  long long in0, in1;
+  long long out;
+  long long ctab;
+  long long part_stride;
+  int nparts;
+  int sgn;
+  int n;
+  int batch;
+  int inverse;
+  int first;     // first work unit (line for rows mode, 32-column tile for cols mode)
+  double scale;
+};
+
+}  // namespace ard

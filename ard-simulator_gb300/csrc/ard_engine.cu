@@ -1,0 +1,290 @@
+// GB300 ARD engine: context creation (work tables, HBM layout), the per-step
+// launch sequence and its CUDA-graph capture, and the C ABI of
+// include/ard_gb300.h for stepping, readout and setup.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ard_device.cuh"
+#include "ard_engine.h"
+#include "ard_gb300.h"
+#include "ard_kernels.cuh"
+
+using namespace ard;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+#define ARD_CUDA(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) {                                                                    \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorName(e_) + " (" + cudaGetErrorString(e_) + ")"; \
+      return e_ == cudaErrorMemoryAllocation ? ARD_ERR_OOM : ARD_ERR_CUDA;                      \
+    }                                                                                           \
+  } while (0)
+
+int grid_for(long long work, int per_block, int max_blocks) {
+  long long b = (work + per_block - 1) / per_block;
+  if (b < 1) b = 1;
+  if (b > max_blocks) b = max_blocks;
+  return (int)b;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// context construction
+// ---------------------------------------------------------------------------
+
+namespace ard {
+
+int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes);
+
+}  // namespace ard
+
+static int validate_scene(const ard_scene& s, std::string* err) {
+  if (!(s.dh > 0) || !(s.dt > 0) || !(s.c0 > 0)) { *err = "scene: dh, dt, c0 must be positive"; return ARD_ERR_INVALID; }
+  if (s.n_partitions < 1 || !s.partitions) { *err = "scene: no partitions"; return ARD_ERR_INVALID; }
+  if (s.pml_layers < 4) { *err = "scene: pml_layers must be >= 4"; return ARD_ERR_INVALID; }
+  // the modal update is exact in time; the PML leapfrog has a CFL bound:
+  // c dt / h <= sqrt(4 / (3 * 1088 / 180 * ... )) ~ 0.470 for the 6th-order Laplacian
+  const double cfl = (double)s.c0 * s.dt / s.dh;
+  if (cfl > 0.4700) {
+    *err = "scene: c0*dt/dh = " + std::to_string(cfl) + " exceeds the 6th-order PML leapfrog limit 0.470";
+    return ARD_ERR_UNSTABLE;
+  }
+  for (int i = 0; i < s.n_partitions; ++i) {
+    const ard_partition& p = s.partitions[i];
+    if (p.width < 1 || p.height < 1 || p.depth < 1) { *err = "scene: empty partition " + std::to_string(i); return ARD_ERR_INVALID; }
+    if (p.kind == ARD_PART_DCT) {
+      if (p.width < 6 || p.height < 6 || p.depth < 6) {
+        *err = "scene: air partition " + std::to_string(i) + " has an extent below 6 cells";
+        return ARD_ERR_INVALID;
+      }
+    } else if (p.kind == ARD_PART_PML) {
+      if (p.pml_type < 0 || p.pml_type > 5) { *err = "scene: bad pml_type"; return ARD_ERR_INVALID; }
+      const int L = (p.pml_type <= 1) ? p.width : (p.pml_type <= 3 ? p.height : p.depth);
+      if (L < 3) { *err = "scene: PML thinner than 3 cells"; return ARD_ERR_INVALID; }
+    } else {
+      *err = "scene: bad partition kind"; return ARD_ERR_INVALID;
+    }
+  }
+  return ARD_OK;
+}
+
+extern "C" int ard_abi_version(void) { return ARD_ABI_VERSION; }
+
+extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_options* opt, ard_ctx** out) {
+  g_create_error.clear();
+  if (!scenes || n_scenes < 1 || !out) { g_create_error = "ard_create: need >= 1 scene and an output pointer"; return ARD_ERR_INVALID; }
+  for (int s = 0; s < n_scenes; ++s) {
+    std::string err;
+    int rc = validate_scene(scenes[s], &err);
+    if (rc) { g_create_error = "scene " + std::to_string(s) + ": " + err; return rc; }
+  }
+  auto ctx = std::make_unique<Ctx>();
+  ctx->prec = opt ? opt->precision : ARD_PREC_F32;
+  ctx->max_steps = (opt && opt->max_steps > 0) ? opt->max_steps : 4096;
+  ctx->use_graphs = opt ? (opt->use_graphs != 0) : true;
+  ctx->device = opt ? opt->device : 0;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    g_create_error = "ard_create: no CUDA device";
+    return ARD_ERR_NOGPU;
+  }
+  if (ctx->device < 0 || ctx->device >= ndev) { g_create_error = "ard_create: bad device ordinal"; return ARD_ERR_INVALID; }
+  if (cudaSetDevice(ctx->device) != cudaSuccess) { g_create_error = "ard_create: cudaSetDevice failed"; return ARD_ERR_CUDA; }
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, ctx->device);
+  if (prop.major * 10 + prop.minor != 103) {
+    g_create_error = "ard_create: kernels are built for sm_103a; device is sm_" + std::to_string(prop.major) + std::to_string(prop.minor);
+    return ARD_ERR_NOGPU;
+  }
+  ctx->num_sms = prop.multiProcessorCount;
+  ctx->smem_optin = (int)prop.sharedMemPerBlockOptin;
+  int rc = build_layout(ctx.get(), scenes, n_scenes);
+  if (rc) {
+    g_create_error = ctx->err;
+    free_ctx_device(ctx.get());
+    return rc;
+  }
+  *out = reinterpret_cast<ard_ctx*>(ctx.release());
+  return ARD_OK;
+}
+
+extern "C" int ard_destroy(ard_ctx* c) {
+  if (!c) return ARD_OK;
+  Ctx* ctx = reinterpret_cast<Ctx*>(c);
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_ctx_device(ctx);
+  delete ctx;
+  return ARD_OK;
+}
+
+extern "C" int ard_last_error(const ard_ctx* c, char* buf, int64_t n) {
+  const std::string& e = c ? reinterpret_cast<const Ctx*>(c)->err : g_create_error;
+  if (buf && n > 0) {
+    const size_t k = std::min<size_t>((size_t)(n - 1), e.size());
+    std::memcpy(buf, e.data(), k);
+    buf[k] = 0;
+  }
+  return ARD_OK;
+}
+
+extern "C" int ard_time_step(const ard_ctx* c, int64_t* out) {
+  if (!c || !out) return ARD_ERR_INVALID;
+  *out = reinterpret_cast<const Ctx*>(c)->t_host;
+  return ARD_OK;
+}
+
+extern "C" int ard_synchronize(ard_ctx* c) {
+  if (!c) return ARD_ERR_INVALID;
+  Ctx* ctx = reinterpret_cast<Ctx*>(c);
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream2));
+  return ARD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// step launches
+// ---------------------------------------------------------------------------
+
+namespace ard {
+
+template <typename T>
+int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, bool fork) {
+  T* buf = reinterpret_cast<T*>(ctx->d_buf);
+  // PML branch depends only on the previous step's interface forcing
+  if (fork) {
+    ARD_CUDA(cudaEventRecord(ctx->ev_fork, s));
+    ARD_CUDA(cudaStreamWaitEvent(s2, ctx->ev_fork, 0));
+  }
+  cudaStream_t sp = fork ? s2 : s;
+  if (ctx->n_pml_cells > 0) {
+    PmlArgs<T> pa{buf, ctx->d_pml, ctx->d_pml_start, (int)ctx->pml.size(), ctx->n_pml_cells, par,
+                  (T)ctx->dt, (T)ctx->dh, (T)ctx->c0};
+    pml_kernel<T><<<grid_for(ctx->n_pml_cells, 256, ctx->num_sms * 16), 256, 0, sp>>>(pa);
+    ARD_CUDA(cudaGetLastError());
+  }
+  if (!ctx->dct.empty()) {
+    const size_t rows_smem = (size_t)8 * ctx->maxn * sizeof(T);
+    const size_t cols_smem = (size_t)33 * ctx->maxn * sizeof(T);
+    xform_rows_kernel<T><<<grid_for(ctx->fwd1.units, 8, ctx->num_sms * 8), 256, rows_smem, s>>>(
+        buf, ctx->d_fwd1, (int)ctx->fwd1.jobs.size(), ctx->fwd1.units, ctx->maxn);
+    ARD_CUDA(cudaGetLastError());
+    xform_cols_kernel<T><<<grid_for(ctx->fwd2.units, 1, ctx->num_sms * 8), 256, cols_smem, s>>>(
+        buf, ctx->d_fwd2, (int)ctx->fwd2.jobs.size(), ctx->fwd2.units);
+    ARD_CUDA(cudaGetLastError());
+    ModalArgs<T> ma{buf, ctx->d_dct, ctx->d_tiles, (int)ctx->tiles.size(), ctx->d_srcpts, ctx->d_recpts,
+                    ctx->d_series, ctx->max_steps, ctx->d_t, tstep, par};
+    modal_kernel<T><<<grid_for((long long)ctx->tiles.size() * 32, 128, 1 << 30), 128, 0, s>>>(ma);
+    ARD_CUDA(cudaGetLastError());
+    if (!ctx->recpts.empty()) {
+      recorder_kernel<T><<<grid_for((long long)ctx->recpts.size() * 32, 128, 1 << 30), 128, 0, s>>>(
+          buf, ctx->d_dct, ctx->d_recpts, (int)ctx->recpts.size(), ctx->d_hist, ctx->d_t, tstep, ctx->max_steps);
+      ARD_CUDA(cudaGetLastError());
+    }
+    xform_cols_kernel<T><<<grid_for(ctx->inv1.units, 1, ctx->num_sms * 8), 256, cols_smem, s>>>(
+        buf, ctx->d_inv1, (int)ctx->inv1.jobs.size(), ctx->inv1.units);
+    ARD_CUDA(cudaGetLastError());
+    xform_rows_kernel<T><<<grid_for(ctx->inv2.units, 8, ctx->num_sms * 8), 256, rows_smem, s>>>(
+        buf, ctx->d_inv2, (int)ctx->inv2.jobs.size(), ctx->inv2.units, ctx->maxn);
+    ARD_CUDA(cudaGetLastError());
+  }
+  if (fork) {
+    ARD_CUDA(cudaEventRecord(ctx->ev_join, s2));
+    ARD_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+  }
+  if (ctx->n_face_cells > 0) {
+    IfaceArgs<T> ia{buf, ctx->d_ifs, (int)ctx->ifs.size(), ctx->n_face_cells, ctx->d_dct, ctx->d_pml,
+                    ctx->d_mask, par, (T)ctx->c0, (T)ctx->dh};
+    iface_kernel<T><<<grid_for(ctx->n_face_cells, 256, ctx->num_sms * 16), 256, 0, s>>>(ia);
+    ARD_CUDA(cudaGetLastError());
+  }
+  return ARD_OK;
+}
+
+template int launch_step<float>(Ctx*, int, int, cudaStream_t, cudaStream_t, bool);
+template int launch_step<double>(Ctx*, int, int, cudaStream_t, cudaStream_t, bool);
+
+int launch_steps_direct(Ctx* ctx, int n, cudaStream_t s) {
+  for (int i = 0; i < n; ++i) {
+    const int par = (int)((ctx->t_host + i) & 1);
+    int rc = ctx->prec == ARD_PREC_F64 ? launch_step<double>(ctx, par, i, s, s, false)
+                                       : launch_step<float>(ctx, par, i, s, s, false);
+    if (rc) return rc;
+  }
+  advance_time_kernel<<<1, 32, 0, s>>>(ctx->d_t, n);
+  ARD_CUDA(cudaGetLastError());
+  ctx->t_host += n;
+  return ARD_OK;
+}
+
+int ensure_graph(Ctx* ctx) {
+  if (ctx->graph_exec) return ARD_OK;
+  cudaGraph_t g = nullptr;
+  ARD_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = ARD_OK;
+  for (int i = 0; i < ctx->graph_steps && rc == ARD_OK; ++i) {
+    rc = ctx->prec == ARD_PREC_F64 ? launch_step<double>(ctx, i & 1, i, ctx->stream, ctx->stream2, true)
+                                   : launch_step<float>(ctx, i & 1, i, ctx->stream, ctx->stream2, true);
+  }
+  if (rc == ARD_OK) advance_time_kernel<<<1, 32, 0, ctx->stream>>>(ctx->d_t, ctx->graph_steps);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+  if (e != cudaSuccess) { ctx->err = std::string("graph capture: ") + cudaGetErrorString(e); return ARD_ERR_CUDA; }
+  e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) { ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e); return ARD_ERR_CUDA; }
+  return ARD_OK;
+}
+
+}  // namespace ard
+
+extern "C" int ard_step(ard_ctx* c, int64_t nsteps, void* stream) {
+  if (!c || nsteps < 0) return ARD_ERR_INVALID;
+  Ctx* ctx = reinterpret_cast<Ctx*>(c);
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  if (s != ctx->stream) {
+    // order the caller's stream after everything queued on ours and vice versa
+    ARD_CUDA(cudaEventRecord(ctx->ev_fork, ctx->stream));
+    ARD_CUDA(cudaStreamWaitEvent(s, ctx->ev_fork, 0));
+  }
+  int64_t left = nsteps;
+  if (ctx->use_graphs && ctx->graph_steps > 0 && left >= ctx->graph_steps) {
+    if (ctx->t_host & 1) {
+      int rc = launch_steps_direct(ctx, 1, s);
+      if (rc) return rc;
+      --left;
+    }
+    int rc = ensure_graph(ctx);
+    if (rc) return rc;
+    while (left >= ctx->graph_steps) {
+      ARD_CUDA(cudaGraphLaunch(ctx->graph_exec, s));
+      ctx->t_host += ctx->graph_steps;
+      left -= ctx->graph_steps;
+    }
+  }
+  if (left > 0) {
+    int rc = launch_steps_direct(ctx, (int)left, s);
+    if (rc) return rc;
+  }
+  if (s != ctx->stream) {
+    ARD_CUDA(cudaEventRecord(ctx->ev_join, s));
+    ARD_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+  }
+  return ARD_OK;
+}

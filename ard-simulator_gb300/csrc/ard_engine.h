@@ -1,0 +1,94 @@
+// Host-side context of the GB300 ARD engine (internal; the public ABI is
+// include/ard_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <string>
+#include <vector>
+
+#include "ard_device.cuh"
+#include "ard_gb300.h"
+
+namespace ard {
+
+struct JobList {
+  std::vector<XformJob> jobs;
+  int units = 0;
+  void add(XformJob j, int units_of_job) {
+    j.first = units;
+    jobs.push_back(j);
+    units += units_of_job;
+  }
+};
+
+struct SceneRec {
+  std::vector<ard_partition> parts;
+  std::vector<int> engine_idx;   // per scene partition: DctDev or PmlDev index
+  int src0 = 0, nsrc = 0;        // global source slots
+  int rec0 = 0, nrec = 0;        // global recorder slots
+  std::array<double, 6> scale{{1, 1, 1, 1, 1, 1}};
+};
+
+struct Ctx {
+  // configuration
+  int prec = ARD_PREC_F32;
+  int device = 0;
+  int num_sms = 1;
+  int smem_optin = 48 * 1024;
+  long long max_steps = 4096;
+  bool use_graphs = true;
+  int graph_steps = 32;
+  double dh = 0, dt = 0, c0 = 0, pml_R = 1e-5, damping = 0.999;
+  int pml_layers = 0;
+  std::string err;
+
+  // work tables (host copies)
+  std::vector<SceneRec> scenes;
+  std::vector<DctDev> dct;
+  std::vector<PmlDev> pml;
+  std::vector<long long> pml_start;
+  std::vector<IfaceDev> ifs;
+  std::vector<unsigned char> masks;
+  std::vector<PointDev> srcpts, recpts;
+  std::vector<int4> tiles;
+  JobList fwd1, fwd2, inv1, inv2;
+  std::vector<std::pair<int, long long>> cos_tables;  // extent -> offset
+  long long n_pml_cells = 0, n_face_cells = 0;
+  long long n_air_cells = 0;
+  int n_src_total = 0, n_rec_total = 0;
+  int maxn = 0;
+  long long pool_elems = 0;
+  long long scratch = 0;          // dense-transform scratch (3 x largest air partition)
+
+  // device memory
+  void* d_buf = nullptr;          // element pool (float or double)
+  unsigned char* d_mask = nullptr;
+  DctDev* d_dct = nullptr;
+  PmlDev* d_pml = nullptr;
+  long long* d_pml_start = nullptr;
+  IfaceDev* d_ifs = nullptr;
+  PointDev* d_srcpts = nullptr;
+  PointDev* d_recpts = nullptr;
+  int4* d_tiles = nullptr;
+  XformJob *d_fwd1 = nullptr, *d_fwd2 = nullptr, *d_inv1 = nullptr, *d_inv2 = nullptr;
+  float* d_series = nullptr;
+  double* d_hist = nullptr;
+  long long* d_t = nullptr;
+
+  cudaStream_t stream = nullptr, stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  long long t_host = 0;
+};
+
+int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes);
+void free_ctx_device(Ctx* ctx);
+template <typename T>
+int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, bool fork);
+int launch_steps_direct(Ctx* ctx, int n, cudaStream_t s);
+int ensure_graph(Ctx* ctx);
+size_t elem_size(const Ctx* ctx);
+
+}  // namespace ard

@@ -1,0 +1,784 @@
+// Context layout: turns flattened scenes (the reference's partitions,
+// boundaries, sources and recorders) into device work tables and an HBM
+// element pool; plus the setup and readout entry points of the C ABI.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "ard_device.cuh"
+#include "ard_engine.h"
+#include "ard_gb300.h"
+#include "ard_kernels.cuh"
+
+using namespace ard;
+
+#define ARD_CUDA(call)                                                                                   \
+  do {                                                                                                   \
+    cudaError_t e_ = (call);                                                                             \
+    if (e_ != cudaSuccess) {                                                                             \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorName(e_) + " (" + cudaGetErrorString(e_) + ")"; \
+      return e_ == cudaErrorMemoryAllocation ? ARD_ERR_OOM : ARD_ERR_CUDA;                               \
+    }                                                                                                    \
+  } while (0)
+
+namespace ard {
+
+size_t elem_size(const Ctx* ctx) { return ctx->prec == ARD_PREC_F64 ? sizeof(double) : sizeof(float); }
+
+namespace {
+
+struct Pool {
+  long long off = 0;
+  long long take(long long n) {
+    const long long o = off;
+    off += (n + 31) / 32 * 32;  // 128-byte (fp32) alignment of every array
+    return o;
+  }
+};
+
+// Face-coordinate view of a partition for an interface of a given type:
+// u fast, v slow, c the crossing axis.
+struct FaceView {
+  int ou, ov, nu, nv, oc, ext;
+};
+
+FaceView face_view(const ard_partition& p, int type) {
+  FaceView f{};
+  if (type == ARD_BOUNDARY_X) { f.ou = p.y_start; f.ov = p.z_start; f.nu = p.height; f.nv = p.depth; f.oc = p.x_start; f.ext = p.width; }
+  else if (type == ARD_BOUNDARY_Y) { f.ou = p.x_start; f.ov = p.z_start; f.nu = p.width; f.nv = p.depth; f.oc = p.y_start; f.ext = p.height; }
+  else { f.ou = p.x_start; f.ov = p.y_start; f.nu = p.width; f.nv = p.height; f.oc = p.z_start; f.ext = p.depth; }
+  return f;
+}
+
+int pml_axis(int pml_type) { return pml_type <= 1 ? ARD_BOUNDARY_X : (pml_type <= 3 ? ARD_BOUNDARY_Y : ARD_BOUNDARY_Z); }
+
+// Reference damping profile of one PML slab (pml_partition.cpp:26-28,59-86)
+// in the context's precision, multiplied by `scale`.
+template <typename R>
+void pml_profile(const Ctx* ctx, int type, int L, double scale, std::vector<double>* out) {
+  const R dh = (R)(float)ctx->dh;
+  const R c0 = (R)(float)ctx->c0;
+  const R Rr = (R)(float)ctx->pml_R;
+  const R thickness = ctx->pml_layers * dh;
+  const R zeta = c0 / thickness * (R)std::log10((R)1 / Rr);
+  const R pi = (R)M_PI;
+  out->assign(L, 0.0);
+  for (int l = 0; l < L; ++l) {
+    // distance index counted from the air side: LEFT/TOP/FRONT use (L - l), others (l + 1)
+    const int s = (type == ARD_PML_LEFT || type == ARD_PML_TOP || type == ARD_PML_FRONT) ? (L - l) : (l + 1);
+    const R z = zeta * (R)scale * (s / thickness * dh - (R)std::sin((R)2 * pi * s * dh / thickness) / (R)2 / pi);
+    (*out)[l] = (double)z;
+  }
+}
+
+}  // namespace
+
+int upload_pml_zeta(Ctx* ctx) {
+  // zeta tables live in the pool; rebuilt whenever a scale changes
+  const size_t es = elem_size(ctx);
+  for (size_t i = 0; i < ctx->pml.size(); ++i) {
+    const PmlDev& P = ctx->pml[i];
+    const double scale = ctx->scenes[P.scene].scale[P.type];
+    std::vector<double> z;
+    if (ctx->prec == ARD_PREC_F64) pml_profile<double>(ctx, P.type, P.L, scale, &z);
+    else pml_profile<float>(ctx, P.type, P.L, scale, &z);
+    if (ctx->prec == ARD_PREC_F64) {
+      ARD_CUDA(cudaMemcpy((char*)ctx->d_buf + P.zeta * es, z.data(), P.L * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+      std::vector<float> zf(z.begin(), z.end());
+      ARD_CUDA(cudaMemcpy((char*)ctx->d_buf + P.zeta * es, zf.data(), P.L * sizeof(float), cudaMemcpyHostToDevice));
+    }
+  }
+  return ARD_OK;
+}
+
+int zero_state(Ctx* ctx) {
+  const size_t es = elem_size(ctx);
+  for (const DctDev& D : ctx->dct) {
+    const long long N = (long long)D.w * D.h * D.d;
+    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.M[0] * es, 0, N * es, ctx->stream));
+    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.M[1] * es, 0, N * es, ctx->stream));
+    const long long faces = 6LL * ((long long)D.d * D.h + (long long)D.d * D.w + (long long)D.h * D.w);
+    // fX..fZ and pX..pZ are contiguous runs of `faces` elements each
+    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.fX * es, 0, (D.fZ - D.fX + 6LL * D.h * D.w) * es, ctx->stream));
+    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.pX * es, 0, (D.pZ - D.pX + 6LL * D.h * D.w) * es, ctx->stream));
+    (void)faces;
+  }
+  for (const PmlDev& P : ctx->pml) {
+    for (int k = 0; k < 2; ++k) {
+      ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + P.p[k] * es, 0, P.n * es, ctx->stream));
+      ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + P.phn[k] * es, 0, P.n * es, ctx->stream));
+      ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + P.pha[k] * es, 0, P.n * es, ctx->stream));
+      ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + P.phb[k] * es, 0, P.n * es, ctx->stream));
+    }
+    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + P.force * es, 0, 3LL * P.A * P.B * es, ctx->stream));
+  }
+  ARD_CUDA(cudaMemsetAsync(ctx->d_t, 0, sizeof(long long), ctx->stream));
+  if (ctx->n_rec_total > 0)
+    ARD_CUDA(cudaMemsetAsync(ctx->d_hist, 0, sizeof(double) * ctx->max_steps * ctx->n_rec_total, ctx->stream));
+  ctx->t_host = 0;
+  return ARD_OK;
+}
+
+int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
+  const ard_scene& s0 = scenes[0];
+  ctx->dh = s0.dh; ctx->dt = s0.dt; ctx->c0 = s0.c0;
+  ctx->pml_layers = s0.pml_layers; ctx->pml_R = s0.pml_R; ctx->damping = s0.modal_damping;
+  for (int s = 1; s < n_scenes; ++s) {
+    const ard_scene& q = scenes[s];
+    if (q.dh != s0.dh || q.dt != s0.dt || q.c0 != s0.c0 || q.pml_layers != s0.pml_layers || q.pml_R != s0.pml_R ||
+        q.modal_damping != s0.modal_damping) {
+      ctx->err = "batched scenes must share dh, dt, c0, pml_layers, pml_R and modal_damping";
+      return ARD_ERR_INVALID;
+    }
+  }
+  Pool pool;
+  std::map<int, long long> cos_off;
+  auto cos_table = [&](int n) {
+    auto it = cos_off.find(n);
+    if (it != cos_off.end()) return it->second;
+    const long long o = pool.take(2LL * n * n);
+    cos_off[n] = o;
+    ctx->maxn = std::max(ctx->maxn, n);
+    return o;
+  };
+
+  // ---- partitions ----
+  std::vector<std::vector<std::vector<int>>> src_by_part;  // [scene][part] -> source indices
+  for (int s = 0; s < n_scenes; ++s) {
+    const ard_scene& sc = scenes[s];
+    SceneRec rec;
+    rec.parts.assign(sc.partitions, sc.partitions + sc.n_partitions);
+    rec.engine_idx.assign(sc.n_partitions, -1);
+    rec.src0 = ctx->n_src_total; rec.nsrc = sc.n_sources;
+    rec.rec0 = ctx->n_rec_total; rec.nrec = sc.n_recorders;
+    ctx->n_src_total += sc.n_sources;
+    ctx->n_rec_total += sc.n_recorders;
+    for (int i = 0; i < sc.n_partitions; ++i) {
+      const ard_partition& p = sc.partitions[i];
+      if (p.kind == ARD_PART_DCT) {
+        DctDev D{};
+        D.w = p.width; D.h = p.height; D.d = p.depth;
+        const long long N = (long long)D.w * D.h * D.d;
+        ctx->n_air_cells += N;
+        D.M[0] = pool.take(N); D.M[1] = pool.take(N);
+        D.cwt = pool.take(N); D.psi = pool.take(N);
+        D.damping = sc.modal_damping;
+        D.sf = 1.0 / (2.0 * std::sqrt(2.0 * (double)N));
+        D.si8 = 1.0 / (8.0 * std::sqrt(2.0 * (double)N));
+        D.cw = cos_table(D.w); D.ch = cos_table(D.h); D.cd = cos_table(D.d);
+        rec.engine_idx[i] = (int)ctx->dct.size();
+        ctx->dct.push_back(D);
+      } else {
+        PmlDev P{};
+        P.type = p.pml_type;
+        P.scene = s;
+        const int ax = pml_axis(p.pml_type);
+        if (ax == ARD_BOUNDARY_X) { P.L = p.width; P.A = p.depth; P.B = p.height; }
+        else if (ax == ARD_BOUNDARY_Y) { P.L = p.height; P.A = p.depth; P.B = p.width; }
+        else { P.L = p.depth; P.A = p.height; P.B = p.width; }
+        P.n = (long long)P.L * P.A * P.B;
+        P.strip0 = -1;
+        rec.engine_idx[i] = (int)ctx->pml.size();
+        ctx->pml.push_back(P);
+      }
+    }
+    ctx->scenes.push_back(rec);
+  }
+
+  // ---- sources / recorders attached to air partitions ----
+  std::vector<std::vector<PointDev>> srcs_of(ctx->dct.size()), recs_of(ctx->dct.size());
+  for (int s = 0; s < n_scenes; ++s) {
+    const ard_scene& sc = scenes[s];
+    const SceneRec& rec = ctx->scenes[s];
+    for (int i = 0; i < sc.n_sources; ++i) {
+      const ard_point& q = sc.sources[i];
+      if (q.partition < 0) continue;  // not inside any air partition: never injected
+      if (q.partition >= sc.n_partitions || sc.partitions[q.partition].kind != ARD_PART_DCT) {
+        ctx->err = "source " + std::to_string(i) + " refers to a partition that is not an air partition";
+        return ARD_ERR_INVALID;
+      }
+      const ard_partition& p = sc.partitions[q.partition];
+      PointDev d{rec.engine_idx[q.partition], q.x - p.x_start, q.y - p.y_start, q.z - p.z_start, rec.src0 + i};
+      if (d.x < 0 || d.y < 0 || d.z < 0 || d.x >= p.width || d.y >= p.height || d.z >= p.depth) {
+        ctx->err = "source " + std::to_string(i) + " lies outside its partition";
+        return ARD_ERR_INVALID;
+      }
+      auto& list = srcs_of[d.part];
+      // two sources on one cell: the later overwrites (partition.cpp:187-197)
+      list.erase(std::remove_if(list.begin(), list.end(),
+                                [&](const PointDev& o) { return o.x == d.x && o.y == d.y && o.z == d.z; }),
+                 list.end());
+      list.push_back(d);
+    }
+    for (int i = 0; i < sc.n_recorders; ++i) {
+      const ard_point& q = sc.recorders[i];
+      if (q.partition < 0 || q.partition >= sc.n_partitions || sc.partitions[q.partition].kind != ARD_PART_DCT) {
+        ctx->err = "recorder " + std::to_string(i) + " is not attached to an air partition";
+        return ARD_ERR_INVALID;
+      }
+      const ard_partition& p = sc.partitions[q.partition];
+      PointDev d{rec.engine_idx[q.partition], q.x - p.x_start, q.y - p.y_start, q.z - p.z_start, rec.rec0 + i};
+      if (d.x < 0 || d.y < 0 || d.z < 0 || d.x >= p.width || d.y >= p.height || d.z >= p.depth) {
+        ctx->err = "recorder " + std::to_string(i) + " lies outside its partition";
+        return ARD_ERR_INVALID;
+      }
+      recs_of[d.part].push_back(d);
+    }
+  }
+  for (size_t k = 0; k < ctx->dct.size(); ++k) {
+    if (srcs_of[k].size() > (size_t)kMaxPointsPerPart || recs_of[k].size() > (size_t)kMaxPointsPerPart) {
+      ctx->err = "more than " + std::to_string(kMaxPointsPerPart) + " sources or recorders in one air partition";
+      return ARD_ERR_INVALID;
+    }
+    DctDev& D = ctx->dct[k];
+    D.src0 = (int)ctx->srcpts.size(); D.nsrc = (int)srcs_of[k].size();
+    ctx->srcpts.insert(ctx->srcpts.end(), srcs_of[k].begin(), srcs_of[k].end());
+    D.rec0 = (int)ctx->recpts.size(); D.nrec = (int)recs_of[k].size();
+    ctx->recpts.insert(ctx->recpts.end(), recs_of[k].begin(), recs_of[k].end());
+  }
+
+  // ---- modal tiling ----
+  long long col_tiles = 0;
+  for (const DctDev& D : ctx->dct) col_tiles += (long long)((D.w + 31) / 32) * ((D.h + kModalTY - 1) / kModalTY);
+  const long long target = (long long)ctx->num_sms * 12;
+  for (size_t k = 0; k < ctx->dct.size(); ++k) {
+    DctDev& D = ctx->dct[k];
+    D.nbx = (D.w + 31) / 32;
+    D.nby = (D.h + kModalTY - 1) / kModalTY;
+    long long nbz = col_tiles > 0 ? (target + col_tiles - 1) / col_tiles : 1;
+    nbz = std::max(1LL, std::min<long long>(nbz, D.d));
+    D.TZ = (int)((D.d + nbz - 1) / nbz);
+    D.nbz = (D.d + D.TZ - 1) / D.TZ;
+    D.tile0 = (int)ctx->tiles.size();
+    for (int bx = 0; bx < D.nbx; ++bx)
+      for (int by = 0; by < D.nby; ++by)
+        for (int bz = 0; bz < D.nbz; ++bz) ctx->tiles.push_back(make_int4((int)k, bx, by, bz));
+    // face arrays
+    const long long FX = 6LL * D.d * D.h, FY = 6LL * D.d * D.w, FZ = 6LL * D.h * D.w;
+    D.fX = pool.off; D.fY = D.fX + FX; D.fZ = D.fY + FY; pool.take(FX + FY + FZ);
+    D.pX = pool.off; D.pY = D.pX + FX; D.pZ = D.pY + FY; pool.take(FX + FY + FZ);
+    D.PX = pool.take(FX); D.PY = pool.take(FY); D.PZ = pool.take(FZ);
+    D.RX = pool.take(FX * D.nbx); D.RY = pool.take(FY * D.nby); D.RZ = pool.take(FZ * D.nbz);
+    D.tmpX = pool.take(FX); D.tmpY = pool.take(FY); D.tmpZ = pool.take(FZ);
+    D.recpart = pool.take(std::max(1, D.nrec) * (long long)D.nbx * D.nby * D.nbz);
+  }
+
+  // ---- dense-transform scratch (initial pressure, field readout): 3 x the largest air partition ----
+  {
+    long long maxN = 0;
+    for (const DctDev& D : ctx->dct) maxN = std::max(maxN, (long long)D.w * D.h * D.d);
+    ctx->scratch = pool.take(3 * maxN);
+  }
+
+  // ---- PML arrays ----
+  for (PmlDev& P : ctx->pml) {
+    for (int k = 0; k < 2; ++k) {
+      P.p[k] = pool.take(P.n); P.phn[k] = pool.take(P.n); P.pha[k] = pool.take(P.n); P.phb[k] = pool.take(P.n);
+    }
+    P.force = pool.take(3LL * P.A * P.B);
+    P.zeta = pool.take(P.L);
+    ctx->pml_start.push_back(ctx->n_pml_cells);
+    ctx->n_pml_cells += P.n;
+  }
+
+  // ---- interfaces + owner masks ----
+  std::vector<std::vector<int>> owner(ctx->dct.size());
+  auto shell_local = [&](int k, int x, int y, int z) {
+    DctDev D = ctx->dct[k];
+    D.fX = 0; D.fY = 6LL * D.d * D.h; D.fZ = D.fY + 6LL * D.d * D.w;
+    return shell_index(D, x, y, z);
+  };
+  for (size_t k = 0; k < ctx->dct.size(); ++k) {
+    const DctDev& D = ctx->dct[k];
+    owner[k].assign(6LL * ((long long)D.d * D.h + (long long)D.d * D.w + (long long)D.h * D.w), -1);
+  }
+  struct PendingIface { IfaceDev dev; int scene; };
+  std::vector<PendingIface> pend;
+  std::vector<int> pml_iface_count(ctx->pml.size(), 0);
+  for (int s = 0; s < n_scenes; ++s) {
+    const ard_scene& sc = scenes[s];
+    const SceneRec& rec = ctx->scenes[s];
+    for (int bi = 0; bi < sc.n_boundaries; ++bi) {
+      const ard_boundary& b = sc.boundaries[bi];
+      if (b.a < 0 || b.b < 0 || b.a >= sc.n_partitions || b.b >= sc.n_partitions || b.type < 0 || b.type > 2) {
+        ctx->err = "boundary " + std::to_string(bi) + ": bad partition index or type";
+        return ARD_ERR_INVALID;
+      }
+      const ard_partition& A = sc.partitions[b.a];
+      const ard_partition& B = sc.partitions[b.b];
+      bool a_lo;
+      int u0, u1, v0, v1;
+      if (b.type == ARD_BOUNDARY_X) {
+        const int ae = A.x_start + A.width;
+        a_lo = (b.x_start <= ae && b.x_end >= ae);
+        u0 = b.y_start; u1 = b.y_end; v0 = b.z_start; v1 = b.z_end;
+      } else if (b.type == ARD_BOUNDARY_Y) {
+        const int ae = A.y_start + A.height;
+        a_lo = (b.y_start <= ae && b.y_end >= ae);
+        u0 = b.x_start; u1 = b.x_end; v0 = b.z_start; v1 = b.z_end;
+      } else {
+        const int ae = A.z_start + A.depth;
+        a_lo = (b.z_start <= ae && b.z_end >= ae);
+        u0 = b.x_start; u1 = b.x_end; v0 = b.y_start; v1 = b.y_end;
+      }
+      if (u1 <= u0 || v1 <= v0) continue;  // empty face: writes nothing
+      const int ilo = a_lo ? b.a : b.b, ihi = a_lo ? b.b : b.a;
+      IfaceDev I{};
+      I.type = b.type; I.u0 = u0; I.u1 = u1; I.v0 = v0; I.v1 = v1;
+      I.absorption = b.absorption;
+      const int sides[2] = {ilo, ihi};
+      for (int side = 0; side < 2; ++side) {
+        const ard_partition& p = sc.partitions[sides[side]];
+        const FaceView f = face_view(p, b.type);
+        SideDev& S = side ? I.hi : I.lo;
+        S.kind = p.kind == ARD_PART_DCT ? 0 : 1;
+        S.idx = rec.engine_idx[sides[side]];
+        S.ou = f.ou; S.ov = f.ov; S.ext = f.ext;
+        S.self = p.kind == ARD_PART_DCT ? 1 : 0;
+        if (u0 < f.ou || u1 > f.ou + f.nu || v0 < f.ov || v1 > f.ov + f.nv || f.ext < 3) {
+          ctx->err = "boundary " + std::to_string(bi) + " reaches outside partition " + std::to_string(sides[side]) +
+                     " (only 2.5D scenes with equal z ranges are supported, as in the reference)";
+          return ARD_ERR_INVALID;
+        }
+        if (S.kind == 1) {
+          PmlDev& P = ctx->pml[S.idx];
+          if (pml_axis(P.type) != b.type) {
+            ctx->err = "boundary " + std::to_string(bi) + " crosses a PML along its plane";
+            return ARD_ERR_INVALID;
+          }
+          const int strip0 = side == 0 ? f.ext - 3 : 0;
+          if (P.strip0 >= 0 && P.strip0 != strip0) {
+            ctx->err = "PML partition forced from both sides";
+            return ARD_ERR_INVALID;
+          }
+          P.strip0 = strip0;
+          pml_iface_count[S.idx]++;
+        }
+      }
+      pend.push_back({I, s});
+    }
+  }
+  // owners in list order: the last interface that writes a shell cell keeps it
+  for (size_t i = 0; i < pend.size(); ++i) {
+    const IfaceDev& I = pend[i].dev;
+    for (int side = 0; side < 2; ++side) {
+      const SideDev& S = side ? I.hi : I.lo;
+      if (S.kind != 0) continue;
+      for (int v = I.v0; v < I.v1; ++v)
+        for (int u = I.u0; u < I.u1; ++u)
+          for (int m = -3; m < 3; ++m) {
+            if ((m < 0) != (side == 0)) continue;
+            const int c = side == 0 ? S.ext + m : m;
+            const int lu = u - S.ou, lv = v - S.ov;
+            const int x = I.type == 0 ? c : lu;
+            const int y = I.type == 0 ? lu : (I.type == 1 ? c : lv);
+            const int z = I.type == 2 ? c : lv;
+            const long long o = shell_local(S.idx, x, y, z);
+            if (o >= 0) owner[S.idx][o] = (int)i;
+          }
+    }
+  }
+  // sources overwrite their cell after every interface (next step's phase A)
+  for (const PointDev& q : ctx->srcpts) {
+    const long long o = shell_local(q.part, q.x, q.y, q.z);
+    if (o >= 0) owner[q.part][o] = -2;
+  }
+  for (size_t i = 0; i < pend.size(); ++i) {
+    IfaceDev I = pend[i].dev;
+    I.mask = (long long)ctx->masks.size();
+    I.cell0 = ctx->n_face_cells;
+    for (int v = I.v0; v < I.v1; ++v)
+      for (int u = I.u0; u < I.u1; ++u) {
+        unsigned char bits = 0;
+        for (int m = -3; m < 3; ++m) {
+          const SideDev& S = m < 0 ? I.lo : I.hi;
+          const int c = m < 0 ? S.ext + m : m;
+          bool on = true;
+          if (S.kind == 0) {
+            const int lu = u - S.ou, lv = v - S.ov;
+            const int x = I.type == 0 ? c : lu;
+            const int y = I.type == 0 ? lu : (I.type == 1 ? c : lv);
+            const int z = I.type == 2 ? c : lv;
+            const long long o = shell_local(S.idx, x, y, z);
+            on = o >= 0 && owner[S.idx][o] == (int)i;
+          }
+          if (on) bits |= (unsigned char)(1u << (m + 3));
+        }
+        ctx->masks.push_back(bits);
+      }
+    ctx->n_face_cells += (long long)(I.u1 - I.u0) * (I.v1 - I.v0);
+    ctx->ifs.push_back(I);
+  }
+  for (size_t k = 0; k < ctx->pml.size(); ++k) {
+    if (pml_iface_count[k] != 1) {
+      ctx->err = "every PML partition needs exactly one interface (found " + std::to_string(pml_iface_count[k]) + ")";
+      return ARD_ERR_INVALID;
+    }
+  }
+
+  // ---- transform jobs ----
+  for (const DctDev& D : ctx->dct) {
+    struct Axis { long long f, p, P, R, tmp; int nU, nV; long long cU, cV; int nb; };
+    const Axis axes[3] = {
+        {D.fX, D.pX, D.PX, D.RX, D.tmpX, D.h, D.d, D.ch, D.cd, D.nbx},
+        {D.fY, D.pY, D.PY, D.RY, D.tmpY, D.w, D.d, D.cw, D.cd, D.nby},
+        {D.fZ, D.pZ, D.PZ, D.RZ, D.tmpZ, D.w, D.h, D.cw, D.ch, D.nbz},
+    };
+    for (const Axis& a : axes) {
+      const long long VU = (long long)a.nU * a.nV;
+      for (int pm = 0; pm < 2; ++pm)
+        for (int n = 0; n < 3; ++n) {
+          XformJob j{};
+          j.in0 = a.f + n * VU; j.in1 = a.f + (5 - n) * VU; j.sgn = pm ? -1 : 1;
+          j.out = a.tmp + (pm * 3 + n) * VU; j.ctab = a.cU; j.n = a.nU; j.batch = a.nV;
+          j.nparts = 1; j.part_stride = 0; j.inverse = 0; j.scale = 1.0;
+          ctx->fwd1.add(j, a.nV);
+          XformJob k{};
+          k.in0 = a.tmp + (pm * 3 + n) * VU; k.in1 = -1; k.sgn = 1;
+          k.out = a.P + (pm * 3 + n) * VU; k.ctab = a.cV; k.n = a.nV; k.batch = a.nU;
+          k.nparts = 1; k.part_stride = 0; k.inverse = 0; k.scale = D.sf;
+          ctx->fwd2.add(k, (a.nU + 31) / 32);
+        }
+      for (int L = 0; L < 6; ++L) {
+        const int n = L < 3 ? L : 5 - L;
+        XformJob j{};
+        j.in0 = a.R + (0 * 3 + n) * VU; j.in1 = a.R + (1 * 3 + n) * VU; j.sgn = L < 3 ? 1 : -1;
+        j.nparts = a.nb; j.part_stride = 6 * VU;
+        j.out = a.tmp + L * VU; j.ctab = a.cV; j.n = a.nV; j.batch = a.nU; j.inverse = 1; j.scale = 1.0;
+        ctx->inv1.add(j, (a.nU + 31) / 32);
+        XformJob k{};
+        k.in0 = a.tmp + L * VU; k.in1 = -1; k.sgn = 1; k.nparts = 1; k.part_stride = 0;
+        k.out = a.p + L * VU; k.ctab = a.cU; k.n = a.nU; k.batch = a.nV; k.inverse = 1; k.scale = D.si8;
+        ctx->inv2.add(k, a.nV);
+      }
+    }
+  }
+
+  // ---- device allocation ----
+  const size_t es = elem_size(ctx);
+  ctx->pool_elems = pool.off;
+  if (33LL * ctx->maxn * (long long)es > ctx->smem_optin) {
+    ctx->err = "partition extent " + std::to_string(ctx->maxn) + " too large for the shared-memory transform tile";
+    return ARD_ERR_INVALID;
+  }
+  ARD_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  ARD_CUDA(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
+  ARD_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+  ARD_CUDA(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+  ARD_CUDA(cudaMalloc(&ctx->d_buf, std::max<size_t>(1, pool.off * es)));
+  ARD_CUDA(cudaMemset(ctx->d_buf, 0, pool.off * es));
+  ARD_CUDA(cudaDeviceSynchronize());
+  auto up = [&](auto** dptr, const auto& vec) -> int {
+    using E = typename std::decay<decltype(vec)>::type::value_type;
+    const size_t bytes = std::max<size_t>(1, vec.size() * sizeof(E));
+    ARD_CUDA(cudaMalloc((void**)dptr, bytes));
+    if (!vec.empty()) ARD_CUDA(cudaMemcpy((void*)*dptr, vec.data(), vec.size() * sizeof(E), cudaMemcpyHostToDevice));
+    return ARD_OK;
+  };
+  int rc;
+  if ((rc = up(&ctx->d_mask, ctx->masks))) return rc;
+  if ((rc = up(&ctx->d_dct, ctx->dct))) return rc;
+  if ((rc = up(&ctx->d_pml, ctx->pml))) return rc;
+  if ((rc = up(&ctx->d_pml_start, ctx->pml_start))) return rc;
+  if ((rc = up(&ctx->d_ifs, ctx->ifs))) return rc;
+  if ((rc = up(&ctx->d_srcpts, ctx->srcpts))) return rc;
+  if ((rc = up(&ctx->d_recpts, ctx->recpts))) return rc;
+  if ((rc = up(&ctx->d_tiles, ctx->tiles))) return rc;
+  if ((rc = up(&ctx->d_fwd1, ctx->fwd1.jobs))) return rc;
+  if ((rc = up(&ctx->d_fwd2, ctx->fwd2.jobs))) return rc;
+  if ((rc = up(&ctx->d_inv1, ctx->inv1.jobs))) return rc;
+  if ((rc = up(&ctx->d_inv2, ctx->inv2.jobs))) return rc;
+  ARD_CUDA(cudaMalloc(&ctx->d_series, sizeof(float) * std::max(1LL, (long long)ctx->n_src_total * ctx->max_steps)));
+  ARD_CUDA(cudaMemset(ctx->d_series, 0, sizeof(float) * (long long)ctx->n_src_total * ctx->max_steps));
+  ARD_CUDA(cudaMalloc(&ctx->d_hist, sizeof(double) * std::max(1LL, (long long)ctx->n_rec_total * ctx->max_steps)));
+  ARD_CUDA(cudaMalloc(&ctx->d_t, sizeof(long long)));
+
+  // ---- tables (FP64 arithmetic on the device) ----
+  for (auto& kv : cos_off) {
+    ctx->cos_tables.push_back(kv);
+    const long long nn = (long long)kv.first * kv.first;
+    const int blocks = (int)std::min<long long>((nn + 255) / 256, 4096);
+    if (ctx->prec == ARD_PREC_F64) cos_table_kernel<double><<<blocks, 256, 0, ctx->stream>>>((double*)ctx->d_buf, kv.second, kv.first);
+    else cos_table_kernel<float><<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, kv.second, kv.first);
+    ARD_CUDA(cudaGetLastError());
+  }
+  for (const DctDev& D : ctx->dct) {
+    const long long N = (long long)D.w * D.h * D.d;
+    const int blocks = (int)std::min<long long>((N + 255) / 256, 8192);
+    if (ctx->prec == ARD_PREC_F64)
+      modal_table_kernel<double><<<blocks, 256, 0, ctx->stream>>>((double*)ctx->d_buf, D.cwt, D.psi, D.w, D.h, D.d,
+                                                                   (double)(float)ctx->dh, (double)(float)ctx->dt,
+                                                                   (double)(float)ctx->c0);
+    else
+      modal_table_kernel<float><<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, D.cwt, D.psi, D.w, D.h, D.d,
+                                                                  (double)(float)ctx->dh, (double)(float)ctx->dt,
+                                                                  (double)(float)ctx->c0);
+    ARD_CUDA(cudaGetLastError());
+  }
+  // the synchronous uploads below run on the legacy stream: finish the table kernels first
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if ((rc = upload_pml_zeta(ctx))) return rc;
+  if ((rc = zero_state(ctx))) return rc;
+  // transform kernels may need more than 48 KB of dynamic shared memory
+  const int cols_smem = (int)(33LL * ctx->maxn * es), rows_smem = (int)(8LL * ctx->maxn * es);
+  if (ctx->prec == ARD_PREC_F64) {
+    ARD_CUDA(cudaFuncSetAttribute(xform_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, cols_smem));
+    ARD_CUDA(cudaFuncSetAttribute(xform_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, rows_smem));
+  } else {
+    ARD_CUDA(cudaFuncSetAttribute(xform_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, cols_smem));
+    ARD_CUDA(cudaFuncSetAttribute(xform_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, rows_smem));
+  }
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  return ARD_OK;
+}
+
+void free_ctx_device(Ctx* ctx) {
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  void* ptrs[] = {ctx->d_buf, ctx->d_mask, ctx->d_dct, ctx->d_pml, ctx->d_pml_start, ctx->d_ifs, ctx->d_srcpts,
+                  ctx->d_recpts, ctx->d_tiles, ctx->d_fwd1, ctx->d_fwd2, ctx->d_inv1, ctx->d_inv2, ctx->d_series,
+                  ctx->d_hist, ctx->d_t};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
+  ctx->graph_exec = nullptr;
+  ctx->d_buf = nullptr;
+}
+
+// Dense 3D transform of one air partition between pool offsets `in` and
+// `out` through a scratch area, with the rows / cols kernels:
+// forward  out = scale * (C_d x C_h x C_w) in          (DCT-II on each axis)
+// inverse  out = scale * (C_d^T x C_h^T x C_w^T) in
+template <typename T>
+int dense_transform(Ctx* ctx, const DctDev& D, long long in, long long out, long long scratch, bool inverse,
+                    double scale) {
+  T* buf = reinterpret_cast<T*>(ctx->d_buf);
+  const long long plane = (long long)D.h * D.w;
+  XformJob base{};
+  base.in1 = -1; base.sgn = 1; base.nparts = 1; base.part_stride = 0; base.inverse = inverse ? 1 : 0;
+  // three passes: x (rows), y (cols per z-slice), z (cols over the plane)
+  JobList px, py, pz;
+  const long long a = in, b = scratch, c = out;
+  // forward order x, y, z; inverse order z, y, x (transposes commute per axis, order is free)
+  {
+    XformJob j = base;
+    j.in0 = a; j.out = b;
+    for (auto& kv : ctx->cos_tables) if (kv.first == D.w) j.ctab = kv.second;
+    j.n = D.w; j.batch = D.d * D.h; j.scale = 1.0;
+    px.add(j, j.batch);
+  }
+  for (int z = 0; z < D.d; ++z) {
+    XformJob j = base;
+    j.in0 = b + z * plane; j.out = c + z * plane;
+    for (auto& kv : ctx->cos_tables) if (kv.first == D.h) j.ctab = kv.second;
+    j.n = D.h; j.batch = D.w; j.scale = 1.0;
+    py.add(j, (D.w + 31) / 32);
+  }
+  {
+    XformJob j = base;
+    j.in0 = c; j.out = b;
+    for (auto& kv : ctx->cos_tables) if (kv.first == D.d) j.ctab = kv.second;
+    j.n = D.d; j.batch = (int)plane; j.scale = scale;
+    pz.add(j, (int)((plane + 31) / 32));
+  }
+  XformJob *dx = nullptr, *dy = nullptr, *dz = nullptr;
+  ARD_CUDA(cudaMalloc(&dx, sizeof(XformJob) * px.jobs.size()));
+  ARD_CUDA(cudaMalloc(&dy, sizeof(XformJob) * py.jobs.size()));
+  ARD_CUDA(cudaMalloc(&dz, sizeof(XformJob) * pz.jobs.size()));
+  ARD_CUDA(cudaMemcpy(dx, px.jobs.data(), sizeof(XformJob) * px.jobs.size(), cudaMemcpyHostToDevice));
+  ARD_CUDA(cudaMemcpy(dy, py.jobs.data(), sizeof(XformJob) * py.jobs.size(), cudaMemcpyHostToDevice));
+  ARD_CUDA(cudaMemcpy(dz, pz.jobs.data(), sizeof(XformJob) * pz.jobs.size(), cudaMemcpyHostToDevice));
+  const size_t rows_smem = (size_t)8 * ctx->maxn * sizeof(T), cols_smem = (size_t)33 * ctx->maxn * sizeof(T);
+  const int gb = ctx->num_sms * 8;
+  xform_rows_kernel<T><<<std::min(gb, (px.units + 7) / 8), 256, rows_smem, ctx->stream>>>(buf, dx, 1, px.units, ctx->maxn);
+  xform_cols_kernel<T><<<std::min(gb, py.units), 256, cols_smem, ctx->stream>>>(buf, dy, (int)py.jobs.size(), py.units);
+  xform_cols_kernel<T><<<std::min(gb, pz.units), 256, cols_smem, ctx->stream>>>(buf, dz, 1, pz.units);
+  ARD_CUDA(cudaGetLastError());
+  // result is in scratch (b); move to out
+  ARD_CUDA(cudaMemcpyAsync(buf + out, buf + b, sizeof(T) * (size_t)D.w * D.h * D.d, cudaMemcpyDeviceToDevice, ctx->stream));
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  cudaFree(dx); cudaFree(dy); cudaFree(dz);
+  return ARD_OK;
+}
+
+template int dense_transform<float>(Ctx*, const DctDev&, long long, long long, long long, bool, double);
+template int dense_transform<double>(Ctx*, const DctDev&, long long, long long, long long, bool, double);
+
+}  // namespace ard
+
+// ---------------------------------------------------------------------------
+// setup / readout entry points
+// ---------------------------------------------------------------------------
+
+static Ctx* as_ctx(ard_ctx* c) { return reinterpret_cast<Ctx*>(c); }
+
+extern "C" int ard_set_source_series(ard_ctx* c, int32_t scene, int32_t source, const float* series, int64_t n) {
+  if (!c) return ARD_ERR_INVALID;
+  Ctx* ctx = as_ctx(c);
+  if (scene < 0 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
+  const SceneRec& s = ctx->scenes[scene];
+  if (source < 0 || source >= s.nsrc) { ctx->err = "bad source index"; return ARD_ERR_RANGE; }
+  if (n < 0 || n > ctx->max_steps || (n > 0 && !series)) { ctx->err = "series longer than max_steps"; return ARD_ERR_RANGE; }
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  float* dst = ctx->d_series + (long long)(s.src0 + source) * ctx->max_steps;
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  ARD_CUDA(cudaMemset(dst, 0, sizeof(float) * ctx->max_steps));
+  if (n > 0) ARD_CUDA(cudaMemcpy(dst, series, sizeof(float) * n, cudaMemcpyHostToDevice));
+  return ARD_OK;
+}
+
+extern "C" int ard_set_pml_scale(ard_ctx* c, int32_t scene, const float scale[6]) {
+  if (!c || !scale) return ARD_ERR_INVALID;
+  Ctx* ctx = as_ctx(c);
+  if (scene < 0 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
+  for (int f = 0; f < 6; ++f) ctx->scenes[scene].scale[f] = scale[f];
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  return ard::upload_pml_zeta(ctx);
+}
+
+extern "C" int ard_reset(ard_ctx* c) {
+  if (!c) return ARD_ERR_INVALID;
+  Ctx* ctx = as_ctx(c);
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  int rc = ard::zero_state(ctx);
+  if (rc) return rc;
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  return ARD_OK;
+}
+
+static int part_lookup(Ctx* ctx, int scene, int part, int* kind, int* idx) {
+  if (scene < 0 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
+  const SceneRec& s = ctx->scenes[scene];
+  if (part < 0 || part >= (int)s.parts.size()) { ctx->err = "bad partition index"; return ARD_ERR_RANGE; }
+  *kind = s.parts[part].kind;
+  *idx = s.engine_idx[part];
+  return ARD_OK;
+}
+
+extern "C" int ard_set_initial_pressure(ard_ctx* c, int32_t scene, int32_t partition, const float* pressure) {
+  if (!c || !pressure) return ARD_ERR_INVALID;
+  Ctx* ctx = as_ctx(c);
+  int kind, idx;
+  int rc = part_lookup(ctx, scene, partition, &kind, &idx);
+  if (rc) return rc;
+  if (kind != ARD_PART_DCT) { ctx->err = "initial pressure applies to air partitions"; return ARD_ERR_INVALID; }
+  if (ctx->t_host != 0) { ctx->err = "initial pressure only before the first step (call ard_reset)"; return ARD_ERR_STATE; }
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  const DctDev& D = ctx->dct[idx];
+  const long long N = (long long)D.w * D.h * D.d;
+  const size_t es = elem_size(ctx);
+  // p0 -> M[1] (host upload), transform in place through the pool scratch, copy the level to M[0]
+  const long long s0 = ctx->scratch;
+  if (ctx->prec == ARD_PREC_F64) {
+    std::vector<double> h(pressure, pressure + N);
+    ARD_CUDA(cudaMemcpy((double*)ctx->d_buf + D.M[1], h.data(), N * es, cudaMemcpyHostToDevice));
+  } else {
+    ARD_CUDA(cudaMemcpy((float*)ctx->d_buf + D.M[1], pressure, N * es, cudaMemcpyHostToDevice));
+  }
+  // modes = DCT-II(p0) / (8 N s_i) with s_i = 1 / sqrt(2N)
+  const double scale = 1.0 / (8.0 * (double)N / std::sqrt(2.0 * (double)N));
+  rc = ctx->prec == ARD_PREC_F64 ? ard::dense_transform<double>(ctx, D, D.M[1], D.M[1], s0, false, scale)
+                                 : ard::dense_transform<float>(ctx, D, D.M[1], D.M[1], s0, false, scale);
+  if (rc == ARD_OK) {
+    cudaError_t e = cudaMemcpy((char*)ctx->d_buf + D.M[0] * es, (char*)ctx->d_buf + D.M[1] * es, N * es, cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = ARD_ERR_CUDA; }
+  }
+  return rc;
+}
+
+extern "C" int ard_read_recorders_f64(ard_ctx* c, int32_t scene, double* out, int64_t t0, int64_t nt) {
+  if (!c || (nt > 0 && !out)) return ARD_ERR_INVALID;
+  Ctx* ctx = as_ctx(c);
+  if (scene < 0 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
+  if (t0 < 0 || nt < 0 || t0 + nt > ctx->t_host || t0 + nt > ctx->max_steps) { ctx->err = "recorder time range not recorded"; return ARD_ERR_RANGE; }
+  const SceneRec& s = ctx->scenes[scene];
+  if (s.nrec == 0 || nt == 0) return ARD_OK;
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<double> h((size_t)nt * ctx->n_rec_total);
+  ARD_CUDA(cudaMemcpy(h.data(), ctx->d_hist + t0 * ctx->n_rec_total, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  bool finite = true;
+  for (int64_t t = 0; t < nt; ++t)
+    for (int r = 0; r < s.nrec; ++r) {
+      const double v = h[(size_t)t * ctx->n_rec_total + s.rec0 + r];
+      out[t * s.nrec + r] = v;
+      finite = finite && std::isfinite(v);
+    }
+  if (!finite) { ctx->err = "non-finite recorder sample (unstable scene?)"; return ARD_ERR_UNSTABLE; }
+  return ARD_OK;
+}
+
+extern "C" int ard_read_recorders(ard_ctx* c, int32_t scene, float* out, int64_t t0, int64_t nt) {
+  if (!c || (nt > 0 && !out)) return ARD_ERR_INVALID;
+  Ctx* ctx = as_ctx(c);
+  if (scene < 0 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
+  const int nrec = ctx->scenes[scene].nrec;
+  std::vector<double> tmp((size_t)std::max<int64_t>(0, nt) * nrec);
+  int rc = ard_read_recorders_f64(c, scene, tmp.data(), t0, nt);
+  for (size_t i = 0; i < tmp.size(); ++i) out[i] = (float)tmp[i];
+  return rc;
+}
+
+extern "C" int ard_read_field(ard_ctx* c, int32_t scene, int32_t partition, float* out) {
+  if (!c || !out) return ARD_ERR_INVALID;
+  Ctx* ctx = as_ctx(c);
+  int kind, idx;
+  int rc = part_lookup(ctx, scene, partition, &kind, &idx);
+  if (rc) return rc;
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  const size_t es = elem_size(ctx);
+  const int lvl = (int)((ctx->t_host - 1) & 1);  // buffer holding the latest level
+  if (kind == ARD_PART_DCT) {
+    const DctDev& D = ctx->dct[idx];
+    const long long N = (long long)D.w * D.h * D.d;
+    const long long s0 = ctx->scratch;
+    char* base = (char*)ctx->d_buf;
+    // copy the modes to the scratch, transform there: p = s_i/8 * C^T C^T C^T M
+    ARD_CUDA(cudaMemcpy(base + (s0 + 2 * N) * es, base + D.M[lvl] * es, N * es, cudaMemcpyDeviceToDevice));
+    rc = ctx->prec == ARD_PREC_F64 ? ard::dense_transform<double>(ctx, D, s0 + 2 * N, s0 + 2 * N, s0, true, D.si8)
+                                   : ard::dense_transform<float>(ctx, D, s0 + 2 * N, s0 + 2 * N, s0, true, D.si8);
+    if (rc == ARD_OK) {
+      if (ctx->prec == ARD_PREC_F64) {
+        std::vector<double> h(N);
+        ARD_CUDA(cudaMemcpy(h.data(), base + (s0 + 2 * N) * es, N * es, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < N; ++i) out[i] = (float)h[i];
+      } else {
+        ARD_CUDA(cudaMemcpy(out, base + (s0 + 2 * N) * es, N * es, cudaMemcpyDeviceToHost));
+      }
+    }
+    return rc;
+  }
+  const PmlDev& P = ctx->pml[idx];
+  const ard_partition& p = ctx->scenes[scene].parts[partition];
+  std::vector<double> h(P.n);
+  if (ctx->prec == ARD_PREC_F64) {
+    ARD_CUDA(cudaMemcpy(h.data(), (char*)ctx->d_buf + P.p[lvl] * es, P.n * es, cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float> f(P.n);
+    ARD_CUDA(cudaMemcpy(f.data(), (char*)ctx->d_buf + P.p[lvl] * es, P.n * es, cudaMemcpyDeviceToHost));
+    h.assign(f.begin(), f.end());
+  }
+  // slab [l][a][b] -> [z][y][x]
+  const int ax = P.type <= 1 ? 0 : (P.type <= 3 ? 1 : 2);
+  for (int z = 0; z < p.depth; ++z)
+    for (int y = 0; y < p.height; ++y)
+      for (int x = 0; x < p.width; ++x) {
+        long long s;
+        if (ax == 0) s = ((long long)x * P.A + z) * P.B + y;
+        else if (ax == 1) s = ((long long)y * P.A + z) * P.B + x;
+        else s = ((long long)z * P.A + y) * P.B + x;
+        out[((long long)z * p.height + y) * p.width + x] = (float)h[s];
+      }
+  return ARD_OK;
+}

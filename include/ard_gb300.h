@@ -216,6 +216,9 @@ int ard_time_step(const ard_ctx* ctx, int64_t* out);
  * (recorder.cpp:40-57) takes it after Simulation::Update.  Synchronous. */
 int ard_read_recorders(ard_ctx* ctx, int32_t scene, float* out, int64_t t0, int64_t nt);
 
+/* Same samples in double precision (the FP64 context keeps them in double). */
+int ard_read_recorders_f64(ard_ctx* ctx, int32_t scene, double* out, int64_t t0, int64_t nt);
+
 /* Current pressure field of partition `partition` of scene `scene`
  * (width*height*depth floats, [z][y][x]).  Synchronous.  For an air
  * partition this runs the full inverse transform of the current modes. */
