@@ -26,7 +26,8 @@
 // 2D transforms of 18 face layers, one fused pass over the modes
 // (expansion of the face transforms along the third axis + modal update +
 // contraction onto the face rows), and 2D inverse transforms of the face
-// layers.  DCT-II basis C_n(k, j) = 2 cos(pi (j + 1/2) k / n) throughout;
+// layers.  Forward basis (REDFT10) C_n(k, j) = 2 cos(pi (j + 1/2) k / n);
+// inverse basis (REDFT01) Ci_n(k, j) = C_n(k, j) with k = 0 halved;
 // C_n(k, n-1-j) = (-1)^k C_n(k, j) pairs layer j with layer 5-j.
 #pragma once
 
@@ -50,10 +51,10 @@ struct DctDev {
   long long PX, PY, PZ;
   long long RX, RY, RZ;
   long long tmpX, tmpY, tmpZ;
-  long long cw, ch, cd;   // cosine tables C[k][j] (n*n) of extents w, h, d
+  long long cw, ch, cd;   // cosine tables of extents w, h, d: C, C^T, Ci (3 n*n each)
   long long recpart;      // [ntiles][nrec] recorder partial sums
   double sf;              // forward scale 1 / (2 sqrt(2N))
-  double si8;             // inverse scale / 8: 1 / (8 sqrt(2N))
+  double si;              // inverse scale 1 / sqrt(2N)
   double damping;
 };
 

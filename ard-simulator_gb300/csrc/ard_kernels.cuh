@@ -59,7 +59,8 @@ __device__ __forceinline__ T job_input(const T* __restrict__ buf, const XformJob
 }
 
 // Rows mode: one warp per line; the line is staged in shared memory.
-// Cosine tables: C[k][j] at ctab, its transpose at ctab + n*n.
+// Forward jobs point ctab at C (transpose at ctab + n*n); inverse jobs point
+// it at the REDFT01 matrix Ci[k][j].
 template <typename T>
 __global__ void __launch_bounds__(256) xform_rows_kernel(T* __restrict__ buf, const XformJob* __restrict__ jobs,
                                                           int njobs, int total, int maxn) {
@@ -165,9 +166,13 @@ __global__ void __launch_bounds__(128) modal_kernel(ModalArgs<T> a) {
   const T* Cw = buf + D.cw;
   const T* Ch = buf + D.ch;
   const T* Cd = buf + D.cd;
-  T cx[3];
+  // REDFT10 row kx for the expansion; REDFT01 weights (k = 0 halved) for the contraction
+  T cx[3], cxi[3];
 #pragma unroll
-  for (int n = 0; n < 3; ++n) cx[n] = Cw[(long long)kxc * w + n];
+  for (int n = 0; n < 3; ++n) {
+    cx[n] = Cw[(long long)kxc * w + n];
+    cxi[n] = kx == 0 ? (T)0.5 * cx[n] : cx[n];
+  }
   const int ky0 = tl.z * TY;
   const int nky = min(TY, h - ky0);
   const int kz0 = tl.w * D.TZ;
@@ -214,16 +219,19 @@ __global__ void __launch_bounds__(128) modal_kernel(ModalArgs<T> a) {
     rxc[r] = 0; racc[r] = 0; ry_[r] = 0; rz_[r] = 0;
     if (r < nrec) {
       const PointDev q = a.recs[D.rec0 + r];
-      rxc[r] = act ? Cw[(long long)kxc * w + q.x] : (T)0;
+      rxc[r] = act ? (kx == 0 ? (T)0.5 : (T)1) * Cw[(long long)kxc * w + q.x] : (T)0;
       ry_[r] = q.y; rz_[r] = q.z;
     }
   }
 
   for (int kz = kz0; kz < kz1; ++kz) {
     const int pzr = kz & 1;
-    T cz[3], py[2][3], ry[2][3];
+    T cz[3], czi[3], py[2][3], ry[2][3];
 #pragma unroll
-    for (int n = 0; n < 3; ++n) cz[n] = Cd[(long long)kz * d + n];
+    for (int n = 0; n < 3; ++n) {
+      cz[n] = Cd[(long long)kz * d + n];
+      czi[n] = kz == 0 ? (T)0.5 * cz[n] : cz[n];
+    }
 #pragma unroll
     for (int pm = 0; pm < 2; ++pm)
 #pragma unroll
@@ -256,15 +264,16 @@ __global__ void __launch_bounds__(128) modal_kernel(ModalArgs<T> a) {
           Mn = (T)D.damping * ((T)2 * c * m - mp + ps * F);
           Mout[idx] = Mn;
         }
+        const T wy = ky == 0 ? (T)0.5 : (T)1;
 #pragma unroll
         for (int n = 0; n < 3; ++n) {
-          rz[i][pzr][n] += cz[n] * Mn;
-          ry[pyr][n] += cy[n] * Mn;
+          rz[i][pzr][n] += czi[n] * Mn;
+          ry[pyr][n] += wy * cy[n] * Mn;
         }
         T v[6];
 #pragma unroll
         for (int n = 0; n < 3; ++n) {
-          const T c = cx[n] * Mn;
+          const T c = cxi[n] * Mn;
           v[n] = px ? (T)0 : c;
           v[3 + n] = px ? c : (T)0;
         }
@@ -279,7 +288,8 @@ __global__ void __launch_bounds__(128) modal_kernel(ModalArgs<T> a) {
         }
 #pragma unroll
         for (int r = 0; r < kMaxPointsPerPart; ++r)
-          if (r < nrec) racc[r] += rxc[r] * (Ch[(long long)ky * h + ry_[r]] * Cd[(long long)kz * d + rz_[r]]) * Mn;
+          if (r < nrec)
+            racc[r] += rxc[r] * (wy * Ch[(long long)ky * h + ry_[r]] * ((kz == 0 ? (T)0.5 : (T)1) * Cd[(long long)kz * d + rz_[r]])) * Mn;
       }
     }
     if (act) {
@@ -328,7 +338,7 @@ __global__ void recorder_kernel(const T* __restrict__ buf, const DctDev* __restr
   for (int i = lane; i < ntiles; i += 32) s += buf[D.recpart + (long long)i * D.nrec + local_r];
   s = warp_sum(s);
   const long long t = *tcount + tstep;
-  if (lane == 0 && t < max_steps) hist[t * nrec_total + q.slot] = (double)(s * (T)D.si8);
+  if (lane == 0 && t < max_steps) hist[t * nrec_total + q.slot] = (double)(s * (T)D.si);
 }
 
 template <typename T>
@@ -511,16 +521,20 @@ static __global__ void advance_time_kernel(long long* tcount, int n) {
 
 // ---- setup kernels (FP64 arithmetic) ----
 
+// Per extent n, three n*n tables: C[k][j] = 2 cos(pi (j + 1/2) k / n) (the
+// REDFT10 matrix), its transpose, and the REDFT01 matrix Ci[k][j] = C[k][j]
+// with row k = 0 halved (REDFT01 weights X_0 by 1, the others by 2).
 template <typename T>
 __global__ void cos_table_kernel(T* buf, long long off, int n) {
   const long long nn = (long long)n * n;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(i / n), j = (int)(i - (long long)k * n);
-    // C[k][j] = 2 cos(pi (j + 1/2) k / n); argument reduced exactly in integers
+    // argument reduced exactly in integers
     const long long q = ((long long)(2 * j + 1) * k) % (4LL * n);
     const double v = 2.0 * cospi((double)q / (2.0 * n));
     buf[off + (long long)k * n + j] = (T)v;
     buf[off + nn + (long long)j * n + k] = (T)v;
+    buf[off + 2 * nn + (long long)k * n + j] = (T)(k == 0 ? 0.5 * v : v);
   }
 }
 

@@ -142,7 +142,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   auto cos_table = [&](int n) {
     auto it = cos_off.find(n);
     if (it != cos_off.end()) return it->second;
-    const long long o = pool.take(2LL * n * n);
+    const long long o = pool.take(3LL * n * n);
     cos_off[n] = o;
     ctx->maxn = std::max(ctx->maxn, n);
     return o;
@@ -170,7 +170,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         D.cwt = pool.take(N); D.psi = pool.take(N);
         D.damping = sc.modal_damping;
         D.sf = 1.0 / (2.0 * std::sqrt(2.0 * (double)N));
-        D.si8 = 1.0 / (8.0 * std::sqrt(2.0 * (double)N));
+        D.si = 1.0 / std::sqrt(2.0 * (double)N);
         D.cw = cos_table(D.w); D.ch = cos_table(D.h); D.cd = cos_table(D.d);
         rec.engine_idx[i] = (int)ctx->dct.size();
         ctx->dct.push_back(D);
@@ -450,11 +450,11 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         XformJob j{};
         j.in0 = a.R + (0 * 3 + n) * VU; j.in1 = a.R + (1 * 3 + n) * VU; j.sgn = L < 3 ? 1 : -1;
         j.nparts = a.nb; j.part_stride = 6 * VU;
-        j.out = a.tmp + L * VU; j.ctab = a.cV; j.n = a.nV; j.batch = a.nU; j.inverse = 1; j.scale = 1.0;
+        j.out = a.tmp + L * VU; j.ctab = a.cV + 2LL * a.nV * a.nV; j.n = a.nV; j.batch = a.nU; j.inverse = 1; j.scale = 1.0;
         ctx->inv1.add(j, (a.nU + 31) / 32);
         XformJob k{};
         k.in0 = a.tmp + L * VU; k.in1 = -1; k.sgn = 1; k.nparts = 1; k.part_stride = 0;
-        k.out = a.p + L * VU; k.ctab = a.cU; k.n = a.nU; k.batch = a.nV; k.inverse = 1; k.scale = D.si8;
+        k.out = a.p + L * VU; k.ctab = a.cU + 2LL * a.nU * a.nU; k.n = a.nU; k.batch = a.nV; k.inverse = 1; k.scale = D.si;
         ctx->inv2.add(k, a.nV);
       }
     }
@@ -555,8 +555,8 @@ void free_ctx_device(Ctx* ctx) {
 
 // Dense 3D transform of one air partition between pool offsets `in` and
 // `out` through a scratch area, with the rows / cols kernels:
-// forward  out = scale * (C_d x C_h x C_w) in          (DCT-II on each axis)
-// inverse  out = scale * (C_d^T x C_h^T x C_w^T) in
+// forward  out = scale * REDFT10 on each axis (matrix C)
+// inverse  out = scale * REDFT01 on each axis (matrix Ci^T)
 template <typename T>
 int dense_transform(Ctx* ctx, const DctDev& D, long long in, long long out, long long scratch, bool inverse,
                     double scale) {
@@ -571,21 +571,21 @@ int dense_transform(Ctx* ctx, const DctDev& D, long long in, long long out, long
   {
     XformJob j = base;
     j.in0 = a; j.out = b;
-    for (auto& kv : ctx->cos_tables) if (kv.first == D.w) j.ctab = kv.second;
+    for (auto& kv : ctx->cos_tables) if (kv.first == D.w) j.ctab = kv.second + (inverse ? 2LL * D.w * D.w : 0);
     j.n = D.w; j.batch = D.d * D.h; j.scale = 1.0;
     px.add(j, j.batch);
   }
   for (int z = 0; z < D.d; ++z) {
     XformJob j = base;
     j.in0 = b + z * plane; j.out = c + z * plane;
-    for (auto& kv : ctx->cos_tables) if (kv.first == D.h) j.ctab = kv.second;
+    for (auto& kv : ctx->cos_tables) if (kv.first == D.h) j.ctab = kv.second + (inverse ? 2LL * D.h * D.h : 0);
     j.n = D.h; j.batch = D.w; j.scale = 1.0;
     py.add(j, (D.w + 31) / 32);
   }
   {
     XformJob j = base;
     j.in0 = c; j.out = b;
-    for (auto& kv : ctx->cos_tables) if (kv.first == D.d) j.ctab = kv.second;
+    for (auto& kv : ctx->cos_tables) if (kv.first == D.d) j.ctab = kv.second + (inverse ? 2LL * D.d * D.d : 0);
     j.n = D.d; j.batch = (int)plane; j.scale = scale;
     pz.add(j, (int)((plane + 31) / 32));
   }
@@ -744,10 +744,10 @@ extern "C" int ard_read_field(ard_ctx* c, int32_t scene, int32_t partition, floa
     const long long N = (long long)D.w * D.h * D.d;
     const long long s0 = ctx->scratch;
     char* base = (char*)ctx->d_buf;
-    // copy the modes to the scratch, transform there: p = s_i/8 * C^T C^T C^T M
+    // copy the modes to the scratch, transform there: p = s_i * Ci^T Ci^T Ci^T M
     ARD_CUDA(cudaMemcpy(base + (s0 + 2 * N) * es, base + D.M[lvl] * es, N * es, cudaMemcpyDeviceToDevice));
-    rc = ctx->prec == ARD_PREC_F64 ? ard::dense_transform<double>(ctx, D, s0 + 2 * N, s0 + 2 * N, s0, true, D.si8)
-                                   : ard::dense_transform<float>(ctx, D, s0 + 2 * N, s0 + 2 * N, s0, true, D.si8);
+    rc = ctx->prec == ARD_PREC_F64 ? ard::dense_transform<double>(ctx, D, s0 + 2 * N, s0 + 2 * N, s0, true, D.si)
+                                   : ard::dense_transform<float>(ctx, D, s0 + 2 * N, s0 + 2 * N, s0, true, D.si);
     if (rc == ARD_OK) {
       if (ctx->prec == ARD_PREC_F64) {
         std::vector<double> h(N);
