@@ -32,6 +32,7 @@ PART_DCT, PART_PML = 0, 1
 PML_LEFT, PML_RIGHT, PML_TOP, PML_BOTTOM, PML_FRONT, PML_BACK = range(6)
 BOUNDARY_X, BOUNDARY_Y, BOUNDARY_Z = range(3)
 PREC_F32, PREC_F64 = 0, 1
+ARITH_ACCURATE, ARITH_REFERENCE = 0, 1
 
 
 class ArdError(RuntimeError):
@@ -73,7 +74,7 @@ class SceneParams(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("max_steps", C.c_int64), ("use_graphs", C.c_int32),
-                ("device", C.c_int32), ("autotune", C.c_int32)]
+                ("device", C.c_int32), ("autotune", C.c_int32), ("arithmetic", C.c_int32)]
 
 
 # Every exported symbol with its ctypes signature (checked against the header by the tests).
@@ -102,6 +103,7 @@ SIGNATURES = {
     "ard_adjoint": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float),
                               C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "ard_read_initial_pressure_grad": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
+    "ard_profile_steps": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "ard_last_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
 }
 
@@ -243,13 +245,14 @@ def scene_from_flat(flat):
 class Simulation:
     """Context over one or many scenes (many = batched mode)."""
 
-    def __init__(self, scenes, precision=PREC_F32, max_steps=4096, use_graphs=True, device=0):
+    def __init__(self, scenes, precision=PREC_F32, max_steps=4096, use_graphs=True, device=0,
+                 arithmetic=ARITH_ACCURATE):
         if isinstance(scenes, Scene):
             scenes = [scenes]
         self.scenes = list(scenes)
         arr = (SceneDesc * len(self.scenes))(*[s.desc for s in self.scenes])
         self._arr = arr
-        opt = Options(precision, max_steps, 1 if use_graphs else 0, device, 0)
+        opt = Options(precision, max_steps, 1 if use_graphs else 0, device, 0, arithmetic)
         h = C.c_void_p()
         _check(lib().ard_create(arr, len(self.scenes), C.byref(opt), C.byref(h)))
         self._h = h
@@ -293,6 +296,14 @@ class Simulation:
         t = self.time_step
         self.run(1)
         return t
+
+    STAGES = ("pml", "fwd_rows", "fwd_cols", "modal", "recorder", "inv_cols", "inv_rows", "iface")
+
+    def profile(self, n, stream=None):
+        """Mean device ms per step of each stage over n un-captured steps."""
+        out = np.zeros(8, np.float32)
+        self._c(lib().ard_profile_steps(self._h, n, stream, _fptr(out), 8))
+        return dict(zip(self.STAGES, out.tolist()))
 
     def synchronize(self):
         self._c(lib().ard_synchronize(self._h))

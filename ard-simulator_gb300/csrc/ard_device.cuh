@@ -5,7 +5,9 @@
 //
 //   air partition (w x h x d cells, N = w*h*d)
 //     M[2][N]        modal amplitudes, two time levels, [kz][ky][kx]
-//     cwt[N], psi[N] cos(w dt) and 2(1-cos(w dt))/w^2, built in FP64
+//     tabA, tabB     modal tables [N]: accurate arithmetic 1-cos(w dt) and
+//                    2(1-cos(w dt))/w^2 built in FP64; reference arithmetic
+//                    cos(w dt) and w^2 as the reference computes them
 //     f{X,Y,Z}       force on the 3-cell shell: X layers [6][d][h] own the
 //                    cells with x in {0,1,2,w-3,w-2,w-1}; Y layers [6][d][w]
 //                    own y in {0,1,2,h-3,h-2,h-1} with x inside; Z layers
@@ -45,7 +47,7 @@ struct DctDev {
   int src0, nsrc;         // attached sources (into PointDev table)
   int rec0, nrec;         // attached recorders
   long long M[2];
-  long long cwt, psi;
+  long long tabA, tabB;
   long long fX, fY, fZ;
   long long pX, pY, pZ;
   long long PX, PY, PZ;

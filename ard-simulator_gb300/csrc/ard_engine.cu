@@ -99,6 +99,11 @@ extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_o
   ctx->max_steps = (opt && opt->max_steps > 0) ? opt->max_steps : 4096;
   ctx->use_graphs = opt ? (opt->use_graphs != 0) : true;
   ctx->device = opt ? opt->device : 0;
+  ctx->arith = opt ? opt->arithmetic : ARD_ARITH_ACCURATE;
+  if (ctx->arith != ARD_ARITH_ACCURATE && ctx->arith != ARD_ARITH_REFERENCE) {
+    g_create_error = "ard_create: bad arithmetic mode";
+    return ARD_ERR_INVALID;
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
     g_create_error = "ard_create: no CUDA device";
@@ -165,15 +170,20 @@ extern "C" int ard_synchronize(ard_ctx* c) {
 
 namespace ard {
 
+// Stage order of one step; with `ev` (kNumStages + 1 events, direct launches
+// on one stream) event k is recorded before stage k and event kNumStages
+// after the last stage.
 template <typename T>
-int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, bool fork) {
+int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, bool fork, cudaEvent_t* ev) {
   T* buf = reinterpret_cast<T*>(ctx->d_buf);
+  auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], s) : cudaSuccess; };
   // PML branch depends only on the previous step's interface forcing
   if (fork) {
     ARD_CUDA(cudaEventRecord(ctx->ev_fork, s));
     ARD_CUDA(cudaStreamWaitEvent(s2, ctx->ev_fork, 0));
   }
   cudaStream_t sp = fork ? s2 : s;
+  ARD_CUDA(mark(kStagePml));
   if (ctx->n_pml_cells > 0) {
     PmlArgs<T> pa{buf, ctx->d_pml, ctx->d_pml_start, (int)ctx->pml.size(), ctx->n_pml_cells, par,
                   (T)ctx->dt, (T)ctx->dh, (T)ctx->c0};
@@ -183,24 +193,33 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   if (!ctx->dct.empty()) {
     const size_t rows_smem = (size_t)8 * ctx->maxn * sizeof(T);
     const size_t cols_smem = (size_t)33 * ctx->maxn * sizeof(T);
+    ARD_CUDA(mark(kStageFwdRows));
     xform_rows_kernel<T><<<grid_for(ctx->fwd1.units, 8, ctx->num_sms * 8), 256, rows_smem, s>>>(
         buf, ctx->d_fwd1, (int)ctx->fwd1.jobs.size(), ctx->fwd1.units, ctx->maxn);
     ARD_CUDA(cudaGetLastError());
+    ARD_CUDA(mark(kStageFwdCols));
     xform_cols_kernel<T><<<grid_for(ctx->fwd2.units, 1, ctx->num_sms * 8), 256, cols_smem, s>>>(
         buf, ctx->d_fwd2, (int)ctx->fwd2.jobs.size(), ctx->fwd2.units);
     ARD_CUDA(cudaGetLastError());
     ModalArgs<T> ma{buf, ctx->d_dct, ctx->d_tiles, (int)ctx->tiles.size(), ctx->d_srcpts, ctx->d_recpts,
                     ctx->d_series, ctx->max_steps, ctx->d_t, tstep, par};
-    modal_kernel<T><<<grid_for((long long)ctx->tiles.size() * 32, 128, 1 << 30), 128, 0, s>>>(ma);
+    ARD_CUDA(mark(kStageModal));
+    if (ctx->arith == ARD_ARITH_REFERENCE)
+      modal_kernel<T, true><<<grid_for((long long)ctx->tiles.size() * 32, 128, 1 << 30), 128, 0, s>>>(ma);
+    else
+      modal_kernel<T, false><<<grid_for((long long)ctx->tiles.size() * 32, 128, 1 << 30), 128, 0, s>>>(ma);
     ARD_CUDA(cudaGetLastError());
+    ARD_CUDA(mark(kStageRecorder));
     if (!ctx->recpts.empty()) {
       recorder_kernel<T><<<grid_for((long long)ctx->recpts.size() * 32, 128, 1 << 30), 128, 0, s>>>(
           buf, ctx->d_dct, ctx->d_recpts, (int)ctx->recpts.size(), ctx->d_hist, ctx->d_t, tstep, ctx->max_steps);
       ARD_CUDA(cudaGetLastError());
     }
+    ARD_CUDA(mark(kStageInvCols));
     xform_cols_kernel<T><<<grid_for(ctx->inv1.units, 1, ctx->num_sms * 8), 256, cols_smem, s>>>(
         buf, ctx->d_inv1, (int)ctx->inv1.jobs.size(), ctx->inv1.units);
     ARD_CUDA(cudaGetLastError());
+    ARD_CUDA(mark(kStageInvRows));
     xform_rows_kernel<T><<<grid_for(ctx->inv2.units, 8, ctx->num_sms * 8), 256, rows_smem, s>>>(
         buf, ctx->d_inv2, (int)ctx->inv2.jobs.size(), ctx->inv2.units, ctx->maxn);
     ARD_CUDA(cudaGetLastError());
@@ -209,23 +228,25 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
     ARD_CUDA(cudaEventRecord(ctx->ev_join, s2));
     ARD_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
   }
+  ARD_CUDA(mark(kStageIface));
   if (ctx->n_face_cells > 0) {
     IfaceArgs<T> ia{buf, ctx->d_ifs, (int)ctx->ifs.size(), ctx->n_face_cells, ctx->d_dct, ctx->d_pml,
                     ctx->d_mask, par, (T)ctx->c0, (T)ctx->dh};
     iface_kernel<T><<<grid_for(ctx->n_face_cells, 256, ctx->num_sms * 16), 256, 0, s>>>(ia);
     ARD_CUDA(cudaGetLastError());
   }
+  ARD_CUDA(mark(kNumStages));
   return ARD_OK;
 }
 
-template int launch_step<float>(Ctx*, int, int, cudaStream_t, cudaStream_t, bool);
-template int launch_step<double>(Ctx*, int, int, cudaStream_t, cudaStream_t, bool);
+template int launch_step<float>(Ctx*, int, int, cudaStream_t, cudaStream_t, bool, cudaEvent_t*);
+template int launch_step<double>(Ctx*, int, int, cudaStream_t, cudaStream_t, bool, cudaEvent_t*);
 
 int launch_steps_direct(Ctx* ctx, int n, cudaStream_t s) {
   for (int i = 0; i < n; ++i) {
     const int par = (int)((ctx->t_host + i) & 1);
-    int rc = ctx->prec == ARD_PREC_F64 ? launch_step<double>(ctx, par, i, s, s, false)
-                                       : launch_step<float>(ctx, par, i, s, s, false);
+    int rc = ctx->prec == ARD_PREC_F64 ? launch_step<double>(ctx, par, i, s, s, false, nullptr)
+                                       : launch_step<float>(ctx, par, i, s, s, false, nullptr);
     if (rc) return rc;
   }
   advance_time_kernel<<<1, 32, 0, s>>>(ctx->d_t, n);
@@ -240,8 +261,8 @@ int ensure_graph(Ctx* ctx) {
   ARD_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   int rc = ARD_OK;
   for (int i = 0; i < ctx->graph_steps && rc == ARD_OK; ++i) {
-    rc = ctx->prec == ARD_PREC_F64 ? launch_step<double>(ctx, i & 1, i, ctx->stream, ctx->stream2, true)
-                                   : launch_step<float>(ctx, i & 1, i, ctx->stream, ctx->stream2, true);
+    rc = ctx->prec == ARD_PREC_F64 ? launch_step<double>(ctx, i & 1, i, ctx->stream, ctx->stream2, true, nullptr)
+                                   : launch_step<float>(ctx, i & 1, i, ctx->stream, ctx->stream2, true, nullptr);
   }
   if (rc == ARD_OK) advance_time_kernel<<<1, 32, 0, ctx->stream>>>(ctx->d_t, ctx->graph_steps);
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
@@ -289,4 +310,43 @@ extern "C" int ard_step(ard_ctx* c, int64_t nsteps, void* stream) {
     ARD_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
   }
   return ARD_OK;
+}
+
+extern "C" int ard_profile_steps(ard_ctx* c, int64_t nsteps, void* stream, float* stage_ms, int32_t nstages) {
+  if (!c || nsteps < 1 || !stage_ms || nstages < kNumStages) return ARD_ERR_INVALID;
+  Ctx* ctx = reinterpret_cast<Ctx*>(c);
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  if (s != ctx->stream) {
+    ARD_CUDA(cudaEventRecord(ctx->ev_fork, ctx->stream));
+    ARD_CUDA(cudaStreamWaitEvent(s, ctx->ev_fork, 0));
+  }
+  std::vector<cudaEvent_t> ev((size_t)nsteps * (kNumStages + 1));
+  for (auto& e : ev) ARD_CUDA(cudaEventCreate(&e));
+  int rc = ARD_OK;
+  for (int64_t i = 0; i < nsteps && rc == ARD_OK; ++i) {
+    const int par = (int)((ctx->t_host + i) & 1);
+    cudaEvent_t* e = ev.data() + i * (kNumStages + 1);
+    rc = ctx->prec == ARD_PREC_F64 ? launch_step<double>(ctx, par, (int)i, s, s, false, e)
+                                   : launch_step<float>(ctx, par, (int)i, s, s, false, e);
+  }
+  if (rc == ARD_OK) {
+    advance_time_kernel<<<1, 32, 0, s>>>(ctx->d_t, (int)nsteps);
+    ctx->t_host += nsteps;
+    cudaError_t err = cudaEventSynchronize(ev.back());
+    for (int k = 0; k < nstages; ++k) stage_ms[k] = 0.f;
+    for (int64_t i = 0; i < nsteps && err == cudaSuccess; ++i)
+      for (int k = 0; k < kNumStages; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[i * (kNumStages + 1) + k], ev[i * (kNumStages + 1) + k + 1]);
+        stage_ms[k] += ms / (float)nsteps;
+      }
+    if (err != cudaSuccess) { ctx->err = cudaGetErrorString(err); rc = ARD_ERR_CUDA; }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (s != ctx->stream && rc == ARD_OK) {
+    ARD_CUDA(cudaEventRecord(ctx->ev_join, s));
+    ARD_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+  }
+  return rc;
 }

@@ -34,6 +34,7 @@ struct SceneRec {
 struct Ctx {
   // configuration
   int prec = ARD_PREC_F32;
+  int arith = ARD_ARITH_ACCURATE;
   int device = 0;
   int num_sms = 1;
   int smem_optin = 48 * 1024;
@@ -83,10 +84,14 @@ struct Ctx {
   long long t_host = 0;
 };
 
+// stages of one step, in launch order (per-stage timing)
+enum { kStagePml = 0, kStageFwdRows, kStageFwdCols, kStageModal, kStageRecorder, kStageInvCols, kStageInvRows,
+       kStageIface, kNumStages };
+
 int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes);
 void free_ctx_device(Ctx* ctx);
 template <typename T>
-int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, bool fork);
+int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, bool fork, cudaEvent_t* ev);
 int launch_steps_direct(Ctx* ctx, int n, cudaStream_t s);
 int ensure_graph(Ctx* ctx);
 size_t elem_size(const Ctx* ctx);

@@ -148,8 +148,9 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// One warp per tile of 32 kx x kModalTY ky x TZ kz modes.
-template <typename T>
+// One warp per tile of 32 kx x kModalTY ky x TZ kz modes.  REF selects the
+// reference's arithmetic (tables cos, w^2) over the accurate one (1-cos, psi).
+template <typename T, bool REF>
 __global__ void __launch_bounds__(128) modal_kernel(ModalArgs<T> a) {
   constexpr int TY = kModalTY;
   const int lane = threadIdx.x & 31;
@@ -179,8 +180,8 @@ __global__ void __launch_bounds__(128) modal_kernel(ModalArgs<T> a) {
   const int kz1 = min(kz0 + D.TZ, d);
   const T* Mcur = buf + D.M[a.par ^ 1];   // M(t-1)
   T* Mout = buf + D.M[a.par];             // holds M(t-2); receives M(t)
-  const T* cwt = buf + D.cwt;
-  const T* psi = buf + D.psi;
+  const T* tabA = buf + D.tabA;
+  const T* tabB = buf + D.tabB;
   const T* PX = buf + D.PX;
   const T* PY = buf + D.PY;
   const T* PZ = buf + D.PZ;
@@ -260,8 +261,11 @@ __global__ void __launch_bounds__(128) modal_kernel(ModalArgs<T> a) {
         const long long idx = ((long long)kz * h + ky) * w + kxc;
         T Mn = 0;
         if (act) {
-          const T m = Mcur[idx], mp = Mout[idx], c = cwt[idx], ps = psi[idx];
-          Mn = (T)D.damping * ((T)2 * c * m - mp + ps * F);
+          const T m = Mcur[idx], mp = Mout[idx], ta = tabA[idx], tb = tabB[idx];
+          if (REF)  // dct_partition.cpp:68: a (2 M cwt - M_prev + (2 F / w2) (1 - cwt))
+            Mn = (T)D.damping * ((T)2 * m * ta - mp + ((T)2 * F / tb) * ((T)1 - ta));
+          else      // same recurrence with ta = 1 - cwt and tb = 2 (1 - cwt) / w2
+            Mn = (T)D.damping * (((T)2 * m - mp) - (T)2 * ta * m + tb * F);
           Mout[idx] = Mn;
         }
         const T wy = ky == 0 ? (T)0.5 : (T)1;
@@ -538,8 +542,10 @@ __global__ void cos_table_kernel(T* buf, long long off, int n) {
   }
 }
 
+// Accurate-arithmetic tables: tabA = 1 - cos(w dt) = 2 sin^2(w dt / 2),
+// tabB = 2 (1 - cos(w dt)) / w^2, in FP64 then rounded to T.
 template <typename T>
-__global__ void modal_table_kernel(T* buf, long long cwt, long long psi, int w, int h, int d, double dh, double dt,
+__global__ void modal_table_kernel(T* buf, long long tabA, long long tabB, int w, int h, int d, double dh, double dt,
                                    double c0) {
   const long long N = (long long)w * h * d;
   const double lx = w * dh, ly = h * dh, lz = d * dh;
@@ -553,8 +559,9 @@ __global__ void modal_table_kernel(T* buf, long long cwt, long long psi, int w, 
     const double omega = c0 * pi * sqrt(az * az + ay * ay + ax * ax);
     const double th = omega * dt;
     const double s = sin(0.5 * th);
-    buf[cwt + i] = (T)cos(th);
-    buf[psi + i] = (T)(4.0 * s * s / (omega * omega));  // 2 (1 - cos th) / omega^2
+    const double vers = 2.0 * s * s;
+    buf[tabA + i] = (T)vers;
+    buf[tabB + i] = (T)(2.0 * vers / (omega * omega));
   }
 }
 

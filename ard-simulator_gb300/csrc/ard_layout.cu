@@ -78,6 +78,31 @@ void pml_profile(const Ctx* ctx, int type, int L, double scale, std::vector<doub
 
 }  // namespace
 
+// Reference-arithmetic modal tables, computed on the host exactly as
+// DctPartition's constructor does (dct_partition.cpp:24-36): 1-based mode
+// numbers, w and cos(w dt) in the working precision with the C library's
+// sqrt / cos; tabA = cos(w dt), tabB = w^2.
+template <typename R>
+int upload_reference_tables(Ctx* ctx, const DctDev& D) {
+  const long long N = (long long)D.w * D.h * D.d;
+  std::vector<R> a((size_t)N), b((size_t)N);
+  const R dh = (R)(float)ctx->dh, dt = (R)(float)ctx->dt, c0 = (R)(float)ctx->c0;
+  const R lx2 = D.w * D.w * dh * dh, ly2 = D.h * D.h * dh * dh, lz2 = D.d * D.d * dh * dh;
+  const R pi = (R)M_PI;
+  for (int i = 1; i <= D.d; ++i)
+    for (int j = 1; j <= D.h; ++j)
+      for (int k = 1; k <= D.w; ++k) {
+        const long long idx = (long long)(i - 1) * D.h * D.w + (long long)(j - 1) * D.w + (k - 1);
+        const R w = c0 * pi * std::sqrt(i * i / lz2 + j * j / ly2 + k * k / lx2);
+        b[idx] = w * w;
+        a[idx] = std::cos(w * dt);
+      }
+  const size_t es = sizeof(R);
+  ARD_CUDA(cudaMemcpy((char*)ctx->d_buf + D.tabA * es, a.data(), N * es, cudaMemcpyHostToDevice));
+  ARD_CUDA(cudaMemcpy((char*)ctx->d_buf + D.tabB * es, b.data(), N * es, cudaMemcpyHostToDevice));
+  return ARD_OK;
+}
+
 int upload_pml_zeta(Ctx* ctx) {
   // zeta tables live in the pool; rebuilt whenever a scale changes
   const size_t es = elem_size(ctx);
@@ -167,7 +192,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         const long long N = (long long)D.w * D.h * D.d;
         ctx->n_air_cells += N;
         D.M[0] = pool.take(N); D.M[1] = pool.take(N);
-        D.cwt = pool.take(N); D.psi = pool.take(N);
+        D.tabA = pool.take(N); D.tabB = pool.take(N);
         D.damping = sc.modal_damping;
         D.sf = 1.0 / (2.0 * std::sqrt(2.0 * (double)N));
         D.si = 1.0 / std::sqrt(2.0 * (double)N);
@@ -510,13 +535,19 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   }
   for (const DctDev& D : ctx->dct) {
     const long long N = (long long)D.w * D.h * D.d;
+    if (ctx->arith == ARD_ARITH_REFERENCE) {
+      ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+      int rc2 = ctx->prec == ARD_PREC_F64 ? upload_reference_tables<double>(ctx, D) : upload_reference_tables<float>(ctx, D);
+      if (rc2) return rc2;
+      continue;
+    }
     const int blocks = (int)std::min<long long>((N + 255) / 256, 8192);
     if (ctx->prec == ARD_PREC_F64)
-      modal_table_kernel<double><<<blocks, 256, 0, ctx->stream>>>((double*)ctx->d_buf, D.cwt, D.psi, D.w, D.h, D.d,
+      modal_table_kernel<double><<<blocks, 256, 0, ctx->stream>>>((double*)ctx->d_buf, D.tabA, D.tabB, D.w, D.h, D.d,
                                                                    (double)(float)ctx->dh, (double)(float)ctx->dt,
                                                                    (double)(float)ctx->c0);
     else
-      modal_table_kernel<float><<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, D.cwt, D.psi, D.w, D.h, D.d,
+      modal_table_kernel<float><<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, D.tabA, D.tabB, D.w, D.h, D.d,
                                                                   (double)(float)ctx->dh, (double)(float)ctx->dt,
                                                                   (double)(float)ctx->c0);
     ARD_CUDA(cudaGetLastError());
@@ -623,13 +654,22 @@ static Ctx* as_ctx(ard_ctx* c) { return reinterpret_cast<Ctx*>(c); }
 extern "C" int ard_set_source_series(ard_ctx* c, int32_t scene, int32_t source, const float* series, int64_t n) {
   if (!c) return ARD_ERR_INVALID;
   Ctx* ctx = as_ctx(c);
+  if (n < 0 || n > ctx->max_steps || (n > 0 && !series)) { ctx->err = "series longer than max_steps"; return ARD_ERR_RANGE; }
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (scene == -1 && source == -1) {
+    // every source of every scene: series is [n_sources_total][n]
+    if (ctx->n_src_total == 0) return ARD_OK;
+    ARD_CUDA(cudaMemset(ctx->d_series, 0, sizeof(float) * ctx->max_steps * ctx->n_src_total));
+    if (n > 0)
+      ARD_CUDA(cudaMemcpy2D(ctx->d_series, sizeof(float) * ctx->max_steps, series, sizeof(float) * n,
+                            sizeof(float) * n, ctx->n_src_total, cudaMemcpyHostToDevice));
+    return ARD_OK;
+  }
   if (scene < 0 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
   const SceneRec& s = ctx->scenes[scene];
   if (source < 0 || source >= s.nsrc) { ctx->err = "bad source index"; return ARD_ERR_RANGE; }
-  if (n < 0 || n > ctx->max_steps || (n > 0 && !series)) { ctx->err = "series longer than max_steps"; return ARD_ERR_RANGE; }
-  ARD_CUDA(cudaSetDevice(ctx->device));
   float* dst = ctx->d_series + (long long)(s.src0 + source) * ctx->max_steps;
-  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
   ARD_CUDA(cudaMemset(dst, 0, sizeof(float) * ctx->max_steps));
   if (n > 0) ARD_CUDA(cudaMemcpy(dst, series, sizeof(float) * n, cudaMemcpyHostToDevice));
   return ARD_OK;
@@ -699,30 +739,26 @@ extern "C" int ard_set_initial_pressure(ard_ctx* c, int32_t scene, int32_t parti
 extern "C" int ard_read_recorders_f64(ard_ctx* c, int32_t scene, double* out, int64_t t0, int64_t nt) {
   if (!c || (nt > 0 && !out)) return ARD_ERR_INVALID;
   Ctx* ctx = as_ctx(c);
-  if (scene < 0 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
+  if (scene < -1 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
   if (t0 < 0 || nt < 0 || t0 + nt > ctx->t_host || t0 + nt > ctx->max_steps) { ctx->err = "recorder time range not recorded"; return ARD_ERR_RANGE; }
-  const SceneRec& s = ctx->scenes[scene];
-  if (s.nrec == 0 || nt == 0) return ARD_OK;
+  const int rec0 = scene < 0 ? 0 : ctx->scenes[scene].rec0;
+  const int nrec = scene < 0 ? ctx->n_rec_total : ctx->scenes[scene].nrec;
+  if (nrec == 0 || nt == 0) return ARD_OK;
   ARD_CUDA(cudaSetDevice(ctx->device));
   ARD_CUDA(cudaStreamSynchronize(ctx->stream));
-  std::vector<double> h((size_t)nt * ctx->n_rec_total);
-  ARD_CUDA(cudaMemcpy(h.data(), ctx->d_hist + t0 * ctx->n_rec_total, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  bool finite = true;
-  for (int64_t t = 0; t < nt; ++t)
-    for (int r = 0; r < s.nrec; ++r) {
-      const double v = h[(size_t)t * ctx->n_rec_total + s.rec0 + r];
-      out[t * s.nrec + r] = v;
-      finite = finite && std::isfinite(v);
-    }
-  if (!finite) { ctx->err = "non-finite recorder sample (unstable scene?)"; return ARD_ERR_UNSTABLE; }
+  // rows of the history are n_rec_total wide; copy only this scene's columns
+  ARD_CUDA(cudaMemcpy2D(out, sizeof(double) * nrec, ctx->d_hist + t0 * ctx->n_rec_total + rec0,
+                        sizeof(double) * ctx->n_rec_total, sizeof(double) * nrec, nt, cudaMemcpyDeviceToHost));
+  for (int64_t i = 0; i < nt * nrec; ++i)
+    if (!std::isfinite(out[i])) { ctx->err = "non-finite recorder sample (unstable scene?)"; return ARD_ERR_UNSTABLE; }
   return ARD_OK;
 }
 
 extern "C" int ard_read_recorders(ard_ctx* c, int32_t scene, float* out, int64_t t0, int64_t nt) {
   if (!c || (nt > 0 && !out)) return ARD_ERR_INVALID;
   Ctx* ctx = as_ctx(c);
-  if (scene < 0 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
-  const int nrec = ctx->scenes[scene].nrec;
+  if (scene < -1 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
+  const int nrec = scene < 0 ? ctx->n_rec_total : ctx->scenes[scene].nrec;
   std::vector<double> tmp((size_t)std::max<int64_t>(0, nt) * nrec);
   int rc = ard_read_recorders_f64(c, scene, tmp.data(), t0, nt);
   for (size_t i = 0; i < tmp.size(); ++i) out[i] = (float)tmp[i];

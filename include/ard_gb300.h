@@ -169,7 +169,18 @@ typedef struct ard_options {
   int32_t use_graphs;    /* capture step sequences in CUDA graphs (default 1) */
   int32_t device;        /* CUDA device ordinal */
   int32_t autotune;      /* pick kernel tile shapes per extent by timing (default 0) */
+  int32_t arithmetic;    /* ARD_ARITH_ACCURATE (default) or ARD_ARITH_REFERENCE */
 } ard_options;
+
+/* Modal-update arithmetic of the air partitions.
+ * ACCURATE: tables 1 - cos(w dt) and 2 (1 - cos(w dt)) / w^2 built in FP64,
+ *   update M+ = a ((2M - M-) - 2 (1 - cos) M + psi F); no cancellation near
+ *   cos = 1, so FP32 stays within 1e-4 of the FP64 solution.
+ * REFERENCE: the reference's own FP32 tables (w and cos(w dt) in float,
+ *   dct_partition.cpp:24-36) and update order (dct_partition.cpp:66-68);
+ *   reproduces the reference's FP32 rounding, whose error against FP64
+ *   reaches ~2e-4 on long runs. */
+enum { ARD_ARITH_ACCURATE = 0, ARD_ARITH_REFERENCE = 1 };
 
 /* Creates a context holding n_scenes independent scenes.  n_scenes > 1 is the
  * batched mode: every stage runs as one launch over all scenes' work tables.
@@ -181,7 +192,9 @@ int ard_destroy(ard_ctx* ctx);
 /* Time series injected by source `source` of scene `scene` (replaces the
  * default all-zero series).  Sample t is written into the force cell at step
  * t, as Partition::ComputeSourceForcingTerms (partition.cpp:187-197) does
- * with SoundSource::SampleValue(t).  n <= max_steps. */
+ * with SoundSource::SampleValue(t).  n <= max_steps.  scene = source = -1
+ * sets every source of every scene at once from series[n_sources_total][n]
+ * (sources numbered scene by scene). */
 int ard_set_source_series(ard_ctx* ctx, int32_t scene, int32_t source,
                           const float* series, int64_t n);
 
@@ -211,7 +224,8 @@ int ard_synchronize(ard_ctx* ctx);
 int ard_time_step(const ard_ctx* ctx, int64_t* out);
 
 /* Recorder samples of scene `scene` for steps t0 .. t0+nt-1, written as
- * out[t][recorder] (n_recorders floats per step).  The sample of step t is
+ * out[t][recorder] (n_recorders floats per step; scene = -1: every recorder
+ * of every scene, numbered scene by scene).  The sample of step t is
  * the pressure after step t's update, as Recorder::RecordField
  * (recorder.cpp:40-57) takes it after Simulation::Update.  Synchronous. */
 int ard_read_recorders(ard_ctx* ctx, int32_t scene, float* out, int64_t t0, int64_t nt);
@@ -243,6 +257,14 @@ int ard_adjoint(ard_ctx* ctx, int64_t T, const float* target,
                 float* grad_source, float* grad_scale, float* loss);
 int ard_read_initial_pressure_grad(ard_ctx* ctx, int32_t scene, int32_t partition,
                                    float* out);
+
+/* Per-stage device time: runs nsteps steps without graph capture on
+ * `stream`, with CUDA events around each kernel, and writes the mean
+ * milliseconds per step of each stage into stage_ms[0..7] in launch order:
+ * PML update, forward face transform (rows, cols), modal update, recorder
+ * sampling, inverse face transform (cols, rows), interface forcing.
+ * nstages >= 8.  The steps count as ordinary steps.  Synchronous. */
+int ard_profile_steps(ard_ctx* ctx, int64_t nsteps, void* stream, float* stage_ms, int32_t nstages);
 
 /* Message of the last error on this context (NULL ctx: last create error). */
 int ard_last_error(const ard_ctx* ctx, char* buf, int64_t n);

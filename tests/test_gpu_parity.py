@@ -1,0 +1,175 @@
+"""GPU parity: the sm_103a path through the C ABI against the reference
+(golden fixtures made by the reference build) and the oracle.
+
+Tolerances: FP32 recorder signals within 1e-4 relative L2 of the reference
+(the spec bar); the FP64 GPU oracle within 1e-10 of the FP64 C oracle
+(same algorithm, different summation order)."""
+import numpy as np
+import pytest
+
+import ard_gb300 as A
+from helpers import load_run, rel_l2
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+F32_TOL = 1e-4
+F64_TOL = 1e-10
+
+
+def gpu_run(sc, series, precision=A.PREC_F32, graphs=True, steps=None, arithmetic=A.ARITH_ACCURATE):
+    p = sc["params"]
+    scene = A.build_scene(sc["air"], sc["sources"], sc["recorders"], p["dh"], p["dt"], p["c0"], p["pml_layers"])
+    T = steps or sc["steps"]
+    sim = A.Simulation(scene, precision=precision, max_steps=T, use_graphs=graphs, arithmetic=arithmetic)
+    for i, s in enumerate(series):
+        sim.set_source_series(i, s[:T])
+    sim.run(T)
+    return scene, sim
+
+
+@pytest.mark.parametrize("arith", [0, 1])
+@pytest.mark.parametrize("name", ["multi4", "scene2_gauss", "quirk_run"])
+def test_recorders_match_reference(name, arith):
+    g = load_run(name)
+    sc = g["scene"]
+    _, sim = gpu_run(sc, g["sources"], arithmetic=arith)
+    got = sim.recorders(f64=True)
+    want = g["recorders"]
+    for r in range(want.shape[1]):
+        if np.isnan(want[0, r]):
+            continue  # recorder outside every partition in the reference run
+        assert rel_l2(got[:, r], want[:, r]) < F32_TOL, (name, r)
+
+
+@pytest.mark.parametrize("name", ["multi4", "quirk_run"])
+def test_fields_match_oracle(name):
+    g = load_run(name)
+    sc = g["scene"]
+    flat = O.make_flat_scene(sc["air"], sc["sources"], sc["recorders"], sc["params"])
+    ref = O.OracleSim(flat, "f32")
+    for i, s in enumerate(g["sources"]):
+        ref.set_source_series(i, s)
+    ref.step(sc["steps"])
+    _, sim = gpu_run(sc, g["sources"])
+    for i, q in enumerate(flat["partitions"]):
+        want = ref.field(i)[0]
+        got = sim.field(i)
+        scale = max(np.abs(want).max(), 1e-30)
+        assert np.abs(got - want).max() / scale < 1e-4, i
+
+
+@pytest.mark.parametrize("name", ["multi4", "quirk_run"])
+def test_fp64_gpu_oracle_matches_fp64_c_oracle(name):
+    g = load_run(name)
+    sc = g["scene"]
+    flat = O.make_flat_scene(sc["air"], sc["sources"], sc["recorders"], sc["params"])
+    ref = O.OracleSim(flat, "f64")
+    for i, s in enumerate(g["sources"]):
+        ref.set_source_series(i, s)
+    ref.step(sc["steps"])
+    want = ref.recorders()
+    _, sim = gpu_run(sc, g["sources"], precision=A.PREC_F64)
+    got = sim.recorders(f64=True)
+    for r in range(want.shape[1]):
+        if np.abs(want[:, r]).max() > 0:
+            assert rel_l2(got[:, r], want[:, r]) < F64_TOL
+
+
+def test_graphs_equal_direct_launches():
+    g = load_run("multi4")
+    _, a = gpu_run(g["scene"], g["sources"], graphs=True)
+    _, b = gpu_run(g["scene"], g["sources"], graphs=False)
+    assert np.array_equal(a.recorders(f64=True), b.recorders(f64=True))
+
+
+def test_reset_reproduces_bitwise_and_update_counts():
+    g = load_run("multi4")
+    sc = g["scene"]
+    _, sim = gpu_run(sc, g["sources"])
+    first = sim.recorders(f64=True)
+    sim.reset()
+    assert sim.time_step == 0
+    assert sim.Update() == 0          # returns the pre-increment index, as Simulation::Update
+    sim.run(sc["steps"] - 1)
+    assert np.array_equal(sim.recorders(f64=True), first)
+
+
+def test_linearity_and_time_shift():
+    """The step is linear in the source series and time-invariant."""
+    g = load_run("multi4")
+    sc = g["scene"]
+    T = sc["steps"]
+    base = [np.asarray(s, np.float32) for s in g["sources"]]
+    _, s1 = gpu_run(sc, base)
+    r1 = s1.recorders(f64=True)
+    _, s2 = gpu_run(sc, [2.0 * s for s in base])
+    assert rel_l2(s2.recorders(f64=True), 2.0 * r1) < 1e-6
+    k = 7
+    shifted = [np.r_[np.zeros(k, np.float32), s[:T - k]] for s in base]
+    _, s3 = gpu_run(sc, shifted)
+    assert rel_l2(s3.recorders(f64=True)[k:], r1[:T - k]) < 1e-5
+
+
+def test_batched_scenes_equal_individual_runs():
+    from ard_gb300 import configs as K
+    cfg = K.config("c2", steps=120)
+    picks = cfg["scenes"][:3]
+    h = float(np.float32(cfg["h"]))
+    scenes = [A.build_scene(s["air"], s["sources"], s["recorders"], h, cfg["dt"], cfg["c0"], cfg["pml"]) for s in picks]
+    batch = A.Simulation(scenes, max_steps=120)
+    for i, s in enumerate(picks):
+        batch.set_source_series(0, s["series"][0], scene=i)
+    batch.run(120)
+    for i, s in enumerate(picks):
+        one = A.Simulation(scenes[i], max_steps=120)
+        one.set_source_series(0, s["series"][0])
+        one.run(120)
+        a, b = batch.recorders(scene=i, f64=True), one.recorders(f64=True)
+        assert rel_l2(a, b) < 1e-6
+    allrec = batch.recorders(scene=-1, f64=True)
+    assert allrec.shape == (120, sum(len(s["recorders"]) for s in picks))
+
+
+def test_initial_pressure_round_trip():
+    sc = A.build_scene([(0, 0, 0, 14, 11, 9)], [(5, 5, 5)], [(7, 6, 6)], 0.1, 1e-4, 343.0, 5)
+    rng = np.random.default_rng(0)
+    p0 = rng.standard_normal((9, 11, 14)).astype(np.float32)
+    for prec in (A.PREC_F32, A.PREC_F64):
+        sim = A.Simulation(sc, precision=prec, max_steps=16)
+        sim.set_initial_pressure(0, p0)
+        got = sim.field(0)
+        tol = 1e-5 if prec == A.PREC_F32 else 1e-7
+        assert np.abs(got - p0).max() < tol * np.abs(p0).max()
+
+
+def test_initial_pressure_dynamics_match_oracle():
+    air, src, rec = [(0, 0, 0, 14, 12, 10), (14, 2, 0, 10, 8, 10)], [(5, 5, 5)], [(8, 6, 5)]
+    h, c = 0.1, 343.0
+    dt = float(np.float32(0.5 * h / (c * np.sqrt(3))))
+    params = dict(dh=h, dt=dt, c0=c, pml_layers=5)
+    flat = O.make_flat_scene(air, src, rec, params)
+    rng = np.random.default_rng(1)
+    p0 = rng.standard_normal((10, 12, 14))
+    ref = O.OracleSim(flat, "f64")
+    ref.set_initial_pressure(0, p0)
+    ref.step(50)
+    sim = A.Simulation(A.build_scene(air, src, rec, h, dt, c, 5), precision=A.PREC_F64, max_steps=50)
+    sim.set_initial_pressure(0, p0.astype(np.float32))
+    sim.run(50)
+    # the float32 upload of p0 limits agreement to ~1e-7
+    assert rel_l2(sim.recorders(f64=True)[:, 0], ref.recorders()[:, 0]) < 1e-6
+
+
+def test_errors_are_reported():
+    g = load_run("multi4")
+    _, sim = gpu_run(g["scene"], g["sources"], steps=10)
+    with pytest.raises(A.ArdError) as e:
+        sim.recorders(t0=0, nt=11)
+    assert e.value.code == 6
+    with pytest.raises(A.ArdError):
+        sim.set_source_series(5, np.zeros(4, np.float32))
+    with pytest.raises(A.ArdError):
+        sim.set_initial_pressure(0, np.zeros((20, 20, 20), np.float32))  # after stepping: state error
+    with pytest.raises(A.ArdError):
+        sim.field(99)
