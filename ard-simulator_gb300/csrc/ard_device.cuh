@@ -1,35 +1,38 @@
 // Device-side work tables of the GB300 ARD engine.
 //
-// Memory layout in HBM (one allocation per element type; every table entry
-// holds element offsets into it):
+// Memory layout in HBM (one allocation per element type; table entries hold
+// element offsets into it).  kx-indexed arrays use the row pitch
+// wp = roundup(w, 4) so that four consecutive modes are one 128-bit access;
+// the padding columns stay zero.
 //
-//   air partition (w x h x d cells, N = w*h*d)
-//     M[2][N]        modal amplitudes, two time levels, [kz][ky][kx]
-//     tabA, tabB     modal tables [N]: accurate arithmetic 1-cos(w dt) and
-//                    2(1-cos(w dt))/w^2 built in FP64; reference arithmetic
-//                    cos(w dt) and w^2 as the reference computes them
-//     f{X,Y,Z}       force on the 3-cell shell: X layers [6][d][h] own the
-//                    cells with x in {0,1,2,w-3,w-2,w-1}; Y layers [6][d][w]
+//   air partition (w x h x d cells)
+//     M[2]           modal amplitudes, two time levels, [kz][ky][wp]
+//     tabA, tabB     modal tables [kz][ky][wp]: accurate arithmetic
+//                    1-cos(w dt) and 2(1-cos(w dt))/w^2 built in FP64;
+//                    reference arithmetic cos(w dt) and w^2 as the
+//                    reference computes them
+//     fX, fY, fZ     force on the 3-cell shell: X layers [6][d][h] own the
+//                    cells with x in {0,1,2,w-3,w-2,w-1}; Y layers [6][d][wp]
 //                    own y in {0,1,2,h-3,h-2,h-1} with x inside; Z layers
-//                    [6][h][w] own z in {0,1,2,d-3,d-2,d-1} with x, y inside
-//     p{X,Y,Z}       pressure on the same face layers, each layer complete
-//     P{X,Y,Z}       2D DCT-II of the force layers, combined as
+//                    [6][h][wp] own z in {0,1,2,d-3,d-2,d-1} with x, y inside
+//     pX, pY, pZ     pressure on the same face layers, each layer complete
+//     PX, PY, PZ     2D DCT-II of the force layers, combined as
 //                    layer(n) +/- layer(5-n): [2][3][..]
-//     R{X,Y,Z}       mode-space contractions onto the face rows, per tile
-//                    partial: [nb][2][3][..]
-//     tmp{X,Y,Z}     transform scratch [6][..]
+//     RX, RY, RZ     contractions of the new modes onto the face rows, one
+//                    slab per modal tile along the contracted axis
+//     tmpX..tmpZ     transform scratch [6][..]
 //   PML slab (L layers along its normal, plane A x B, B fastest)
 //     p[2], phi_n[2], phi_a[2], phi_b[2]   [L][A][B]
 //     force strip    [3][A][B] (the 3 layers next to the air partition)
 //
 // The modal update of an air partition needs the force only on the shell and
 // yields pressure only where the interfaces (shell) and recorders read it, so
-// the dense 3D DCT pair of the reference (dct_partition.cpp:48-73) becomes:
-// 2D transforms of 18 face layers, one fused pass over the modes
-// (expansion of the face transforms along the third axis + modal update +
-// contraction onto the face rows), and 2D inverse transforms of the face
-// layers.  Forward basis (REDFT10) C_n(k, j) = 2 cos(pi (j + 1/2) k / n);
-// inverse basis (REDFT01) Ci_n(k, j) = C_n(k, j) with k = 0 halved;
+// the dense 3D DCT pair of the reference (dct_partition.cpp:48-73) becomes
+// 2D transforms of 18 face layers, one fused pass over the modes (expansion
+// of the face transforms along the third axis + modal update + contraction
+// onto the face rows) and 2D inverse transforms of the face layers.
+// Forward basis (REDFT10) C_n(k, j) = 2 cos(pi (j + 1/2) k / n); inverse
+// basis (REDFT01) Ci_n(k, j) = C_n(k, j) with k = 0 halved;
 // C_n(k, n-1-j) = (-1)^k C_n(k, j) pairs layer j with layer 5-j.
 #pragma once
 
@@ -37,15 +40,17 @@
 
 namespace ard {
 
-constexpr int kMaxPointsPerPart = 8;  // sources or recorders per air partition per modal tile
-constexpr int kModalTY = 4;           // ky rows per warp tile of the modal kernel
+constexpr int kMaxPointsPerPart = 8;  // sources or recorders per air partition
+constexpr int kModalThreads = 256;    // 8 warps per modal tile
+constexpr int kMaxPmlLayers = 12;
 
 struct DctDev {
-  int w, h, d;
-  int nbx, nby, nbz, TZ;  // modal tiling: 32-wide kx chunks, TY ky rows, TZ kz planes
-  int tile0;              // index of this partition's first modal tile
-  int src0, nsrc;         // attached sources (into PointDev table)
-  int rec0, nrec;         // attached recorders
+  int w, h, d, wp;
+  int G, rpc, kxt;         // lanes per ky row, ky rows per tile, kx per tile (4 G)
+  int nbx, nby, nbz, TZ;   // tiles along kx, ky, kz
+  int tile0;
+  int src0, nsrc;          // attached sources (PointDev table)
+  int rec0, nrec;          // attached recorders
   long long M[2];
   long long tabA, tabB;
   long long fX, fY, fZ;
@@ -53,10 +58,10 @@ struct DctDev {
   long long PX, PY, PZ;
   long long RX, RY, RZ;
   long long tmpX, tmpY, tmpZ;
-  long long cw, ch, cd;   // cosine tables of extents w, h, d: C, C^T, Ci (3 n*n each)
-  long long recpart;      // [ntiles][nrec] recorder partial sums
-  double sf;              // forward scale 1 / (2 sqrt(2N))
-  double si;              // inverse scale 1 / sqrt(2N)
+  long long cw, ch, cd;    // cosine tables of extents w, h, d: C then Ci (n*n each)
+  long long recpart;       // [ntiles][nrec]
+  double sf;               // forward scale 1 / (2 sqrt(2N))
+  double si;               // inverse scale 1 / sqrt(2N)
   double damping;
 };
 
@@ -97,12 +102,12 @@ struct IfaceDev {
   long long cell0;        // first global face-cell index of this interface
 };
 
-// One batched 1D transform job over lines of a 2D array.
-//   rows mode: lines are contiguous rows, array [batch][n]
-//   cols mode: lines are columns, array [n][batch]
-// Input = sum over `nparts` partial slabs (stride part_stride) of
-// in0 + sgn * in1 (in1 < 0: absent).  Forward: out_k = scale sum_j C[k][j] x_j;
-// inverse: out_j = scale sum_k C[k][j] x_k.
+// One batched 1D transform as a small GEMM, Out[m][nn] (row pitch ld):
+//   cols (rows == 0): lines are columns of [n][ld];  Out = A X,   M = n, N = batch
+//   rows (rows == 1): lines are rows of [batch][ld]; Out = X A^T, M = batch, N = n
+// A(o, j) = C[o][j] (forward, REDFT10) or Ci[j][o] (inverse, REDFT01); ctab
+// points at the matrix used.  X = sum over `nparts` slabs (stride
+// part_stride) of in0 + sgn * in1 (in1 < 0: absent).
 struct XformJob {
   long long in0, in1;
   long long out;
@@ -112,8 +117,12 @@ struct XformJob {
   int sgn;
   int n;
   int batch;
+  int ld;
   int inverse;
-  int first;     // first work unit (line for rows mode, 32-column tile for cols mode)
+  int rows;
+  int first;    // first 64 x 64 output tile of this job
+  int tn;       // tiles along N
+  int ntiles;
   double scale;
 };
 

@@ -184,30 +184,31 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   }
   cudaStream_t sp = fork ? s2 : s;
   ARD_CUDA(mark(kStagePml));
-  if (ctx->n_pml_cells > 0) {
-    PmlArgs<T> pa{buf, ctx->d_pml, ctx->d_pml_start, (int)ctx->pml.size(), ctx->n_pml_cells, par,
+  if (!ctx->pml_blocks.empty()) {
+    PmlArgs<T> pa{buf, ctx->d_pml, ctx->d_pml_blocks, (int)ctx->pml_blocks.size(), par,
                   (T)ctx->dt, (T)ctx->dh, (T)ctx->c0};
-    pml_kernel<T><<<grid_for(ctx->n_pml_cells, 256, ctx->num_sms * 16), 256, 0, sp>>>(pa);
+    pml_kernel<T><<<grid_for((long long)ctx->pml_blocks.size(), 1, ctx->num_sms * 8), 256, 0, sp>>>(pa);
     ARD_CUDA(cudaGetLastError());
   }
   if (!ctx->dct.empty()) {
-    const size_t rows_smem = (size_t)8 * ctx->maxn * sizeof(T);
-    const size_t cols_smem = (size_t)33 * ctx->maxn * sizeof(T);
+    const int gx = ctx->num_sms * 4;
     ARD_CUDA(mark(kStageFwdRows));
-    xform_rows_kernel<T><<<grid_for(ctx->fwd1.units, 8, ctx->num_sms * 8), 256, rows_smem, s>>>(
-        buf, ctx->d_fwd1, (int)ctx->fwd1.jobs.size(), ctx->fwd1.units, ctx->maxn);
+    xform_gemm_kernel<T><<<grid_for(ctx->fwd1.units, 1, gx), 256, 0, s>>>(buf, ctx->d_fwd1, (int)ctx->fwd1.jobs.size(),
+                                                                           ctx->fwd1.units);
     ARD_CUDA(cudaGetLastError());
     ARD_CUDA(mark(kStageFwdCols));
-    xform_cols_kernel<T><<<grid_for(ctx->fwd2.units, 1, ctx->num_sms * 8), 256, cols_smem, s>>>(
-        buf, ctx->d_fwd2, (int)ctx->fwd2.jobs.size(), ctx->fwd2.units);
+    xform_gemm_kernel<T><<<grid_for(ctx->fwd2.units, 1, gx), 256, 0, s>>>(buf, ctx->d_fwd2, (int)ctx->fwd2.jobs.size(),
+                                                                           ctx->fwd2.units);
     ARD_CUDA(cudaGetLastError());
     ModalArgs<T> ma{buf, ctx->d_dct, ctx->d_tiles, (int)ctx->tiles.size(), ctx->d_srcpts, ctx->d_recpts,
                     ctx->d_series, ctx->max_steps, ctx->d_t, tstep, par};
     ARD_CUDA(mark(kStageModal));
+    const size_t msmem = kModalSmemElems * sizeof(T);
+    const int mgrid = grid_for((long long)ctx->tiles.size(), 1, ctx->num_sms * 2);
     if (ctx->arith == ARD_ARITH_REFERENCE)
-      modal_kernel<T, true><<<grid_for((long long)ctx->tiles.size() * 32, 128, 1 << 30), 128, 0, s>>>(ma);
+      modal_kernel<T, true><<<mgrid, kModalThreads, msmem, s>>>(ma);
     else
-      modal_kernel<T, false><<<grid_for((long long)ctx->tiles.size() * 32, 128, 1 << 30), 128, 0, s>>>(ma);
+      modal_kernel<T, false><<<mgrid, kModalThreads, msmem, s>>>(ma);
     ARD_CUDA(cudaGetLastError());
     ARD_CUDA(mark(kStageRecorder));
     if (!ctx->recpts.empty()) {
@@ -216,12 +217,12 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
       ARD_CUDA(cudaGetLastError());
     }
     ARD_CUDA(mark(kStageInvCols));
-    xform_cols_kernel<T><<<grid_for(ctx->inv1.units, 1, ctx->num_sms * 8), 256, cols_smem, s>>>(
-        buf, ctx->d_inv1, (int)ctx->inv1.jobs.size(), ctx->inv1.units);
+    xform_gemm_kernel<T><<<grid_for(ctx->inv1.units, 1, gx), 256, 0, s>>>(buf, ctx->d_inv1, (int)ctx->inv1.jobs.size(),
+                                                                           ctx->inv1.units);
     ARD_CUDA(cudaGetLastError());
     ARD_CUDA(mark(kStageInvRows));
-    xform_rows_kernel<T><<<grid_for(ctx->inv2.units, 8, ctx->num_sms * 8), 256, rows_smem, s>>>(
-        buf, ctx->d_inv2, (int)ctx->inv2.jobs.size(), ctx->inv2.units, ctx->maxn);
+    xform_gemm_kernel<T><<<grid_for(ctx->inv2.units, 1, gx), 256, 0, s>>>(buf, ctx->d_inv2, (int)ctx->inv2.jobs.size(),
+                                                                           ctx->inv2.units);
     ARD_CUDA(cudaGetLastError());
   }
   if (fork) {

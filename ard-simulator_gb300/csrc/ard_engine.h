@@ -49,7 +49,7 @@ struct Ctx {
   std::vector<SceneRec> scenes;
   std::vector<DctDev> dct;
   std::vector<PmlDev> pml;
-  std::vector<long long> pml_start;
+  std::vector<int4> pml_blocks;
   std::vector<IfaceDev> ifs;
   std::vector<unsigned char> masks;
   std::vector<PointDev> srcpts, recpts;
@@ -68,7 +68,7 @@ struct Ctx {
   unsigned char* d_mask = nullptr;
   DctDev* d_dct = nullptr;
   PmlDev* d_pml = nullptr;
-  long long* d_pml_start = nullptr;
+  int4* d_pml_blocks = nullptr;
   IfaceDev* d_ifs = nullptr;
   PointDev* d_srcpts = nullptr;
   PointDev* d_recpts = nullptr;

@@ -2,20 +2,23 @@
 // (float: the product path; double: the FP64 GPU oracle).
 //
 // Per step (t, parity par = t & 1):
-//   xform_rows / xform_cols   forward 2D DCT-II of the 18 force face layers
-//   modal_kernel              F = expansion of the face transforms (+ point
-//                             sources); M(t) = a (2 cwt M(t-1) - M(t-2) + psi F);
-//                             contraction of M(t) onto the face rows and the
-//                             recorder cells
-//   recorder_kernel           recorder samples of step t
-//   xform_cols / xform_rows   inverse 2D transforms -> pressure face layers
-//   pml_kernel                Grote-Sim PML update of every slab
-//   iface_kernel              6th-order interface forcing into the force
-//                             face layers / PML strips (owner masks resolve
-//                             overlapping strips in reference list order)
+//   xform_gemm_kernel   forward 2D DCT-II of the 18 force face layers of every
+//                       air partition (two batched GEMM passes)
+//   modal_kernel        F = expansion of the face transforms (+ point
+//                       sources); M(t) = a (2 cos M(t-1) - M(t-2) + psi F);
+//                       contraction of M(t) onto the face rows and the
+//                       recorder cells
+//   recorder_kernel     recorder samples of step t
+//   xform_gemm_kernel   inverse 2D transforms -> pressure face layers
+//   pml_kernel          Grote-Sim PML update of every slab
+//   iface_kernel        6th-order interface forcing into the force face
+//                       layers / PML strips (owner masks resolve overlapping
+//                       strips in the reference's list order)
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "ard_device.cuh"
 
@@ -32,11 +35,41 @@ __host__ __device__ inline long long shell_index(const DctDev& D, int x, int y, 
   int l = face_layer(x, D.w);
   if (l >= 0) return D.fX + ((long long)l * D.d + z) * D.h + y;
   l = face_layer(y, D.h);
-  if (l >= 0) return D.fY + ((long long)l * D.d + z) * D.w + x;
+  if (l >= 0) return D.fY + ((long long)l * D.d + z) * D.wp + x;
   l = face_layer(z, D.d);
-  if (l >= 0) return D.fZ + ((long long)l * D.h + y) * D.w + x;
+  if (l >= 0) return D.fZ + ((long long)l * D.h + y) * D.wp + x;
   return -1;
 }
+
+// ---- 4-wide vector access (128-bit for float, 2 x 128-bit for double) ----
+__device__ __forceinline__ void load4(const float* p, float (&r)[4]) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+}
+__device__ __forceinline__ void load4(const double* p, double (&r)[4]) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+  r[0] = a.x; r[1] = a.y; r[2] = b.x; r[3] = b.y;
+}
+__device__ __forceinline__ void store4(float* p, const float (&r)[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(r[0], r[1], r[2], r[3]);
+}
+__device__ __forceinline__ void store4(double* p, const double (&r)[4]) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(r[0], r[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(r[2], r[3]);
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Face transforms: every job is a small GEMM (see XformJob); one 64 x 64
+// output tile per block iteration, K staged through shared memory in chunks
+// of 16, 4 x 4 outputs per thread.
+// ---------------------------------------------------------------------------
 
 __device__ __forceinline__ int find_job(const XformJob* __restrict__ jobs, int njobs, int unit) {
   int lo = 0, hi = njobs - 1;
@@ -58,269 +91,335 @@ __device__ __forceinline__ T job_input(const T* __restrict__ buf, const XformJob
   return v;
 }
 
-// Rows mode: one warp per line; the line is staged in shared memory.
-// Forward jobs point ctab at C (transpose at ctab + n*n); inverse jobs point
-// it at the REDFT01 matrix Ci[k][j].
 template <typename T>
-__global__ void __launch_bounds__(256) xform_rows_kernel(T* __restrict__ buf, const XformJob* __restrict__ jobs,
-                                                          int njobs, int total, int maxn) {
-  extern __shared__ unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  T* row = reinterpret_cast<T*>(smem_raw) + (long long)warp * maxn;
-  for (int unit = blockIdx.x * nwarps + warp; unit < total; unit += gridDim.x * nwarps) {
+__global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, const XformJob* __restrict__ jobs,
+                                                          int njobs, int total) {
+  __shared__ T Ps[16][64 + 4];  // P(m0 + mm, k0 + kk) at [kk][mm]
+  __shared__ T Qs[16][64 + 4];  // Q(k0 + kk, n0 + nn) at [kk][nn]
+  const int tid = threadIdx.x;
+  const int ty = tid >> 4, tx = tid & 15;
+  for (int unit = blockIdx.x; unit < total; unit += gridDim.x) {
     const XformJob J = jobs[find_job(jobs, njobs, unit)];
-    const int line = unit - J.first;
-    const int n = J.n;
-    const long long lbase = (long long)line * n;
-    for (int j = lane; j < n; j += 32) row[j] = job_input(buf, J, lbase + j);
-    __syncwarp();
-    const T scale = (T)J.scale;
-    const T* C = buf + J.ctab;
-    if (!J.inverse) {
-      const T* Ct = C + (long long)n * n;
-      for (int k = lane; k < n; k += 32) {
-        T acc = 0;
-        for (int j = 0; j < n; ++j) acc += Ct[(long long)j * n + k] * row[j];
-        buf[J.out + lbase + k] = acc * scale;
+    const int t = unit - J.first;
+    const int m0 = (t / J.tn) * 64, n0 = (t % J.tn) * 64;
+    const int Md = J.rows ? J.batch : J.n;
+    const int Nd = J.rows ? J.n : J.batch;
+    const int K = J.n;
+    const T* A = buf + J.ctab;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = 0;
+    for (int k0 = 0; k0 < K; k0 += 16) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int e = tid + 256 * r;
+        if (!J.rows) {
+          // P = A (m = output o, k = j); Q = X (k = j, n = column)
+          const int mm = J.inverse ? (e & 63) : (e >> 4), kk = J.inverse ? (e >> 6) : (e & 15);
+          const int m = m0 + mm, k = k0 + kk;
+          T pv = 0;
+          if (m < Md && k < K) pv = J.inverse ? A[(long long)k * K + m] : A[(long long)m * K + k];
+          Ps[kk][mm] = pv;
+          const int nn = e & 63, kq = e >> 6;
+          const int n = n0 + nn, kk2 = k0 + kq;
+          Qs[kq][nn] = (n < Nd && kk2 < K) ? job_input(buf, J, (long long)kk2 * J.ld + n) : (T)0;
+        } else {
+          // P = X (m = line, k = j); Q(k, n) = A(n, k)
+          const int mm = e >> 4, kk = e & 15;
+          const int m = m0 + mm, k = k0 + kk;
+          Ps[kk][mm] = (m < Md && k < K) ? job_input(buf, J, (long long)m * J.ld + k) : (T)0;
+          const int nn = J.inverse ? (e & 63) : (e >> 4), kq = J.inverse ? (e >> 6) : (e & 15);
+          const int n = n0 + nn, kk2 = k0 + kq;
+          T qv = 0;
+          if (n < Nd && kk2 < K) qv = J.inverse ? A[(long long)kk2 * K + n] : A[(long long)n * K + kk2];
+          Qs[kq][nn] = qv;
+        }
       }
-    } else {
-      for (int j = lane; j < n; j += 32) {
-        T acc = 0;
-        for (int k = 0; k < n; ++k) acc += C[(long long)k * n + j] * row[k];
-        buf[J.out + lbase + j] = acc * scale;
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < 16; ++kk) {
+        T pa[4], qb[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) pa[i] = Ps[kk][ty * 4 + i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) qb[j] = Qs[kk][tx * 4 + j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] += pa[i] * qb[j];
+      }
+      __syncthreads();
+    }
+    const T scale = (T)J.scale;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int m = m0 + ty * 4 + i;
+      if (m >= Md) continue;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int n = n0 + tx * 4 + j;
+        if (n < Nd) buf[J.out + (long long)m * J.ld + n] = acc[i][j] * scale;
       }
     }
-    __syncwarp();
   }
 }
 
-// Cols mode: one block per 32-column tile; the [n][32] tile is staged in
-// shared memory (row pitch 33), warps split the outputs.
-template <typename T>
-__global__ void __launch_bounds__(256) xform_cols_kernel(T* __restrict__ buf, const XformJob* __restrict__ jobs,
-                                                          int njobs, int total) {
-  extern __shared__ unsigned char smem_raw[];
-  T* tile = reinterpret_cast<T*>(smem_raw);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (int unit = blockIdx.x; unit < total; unit += gridDim.x) {
-    const XformJob J = jobs[find_job(jobs, njobs, unit)];
-    const int col = (unit - J.first) * 32 + lane;
-    const bool act = col < J.batch;
-    const int n = J.n;
-    for (int j = warp; j < n; j += nwarps)
-      tile[j * 33 + lane] = act ? job_input(buf, J, (long long)j * J.batch + col) : (T)0;
-    __syncthreads();
-    const T scale = (T)J.scale;
-    const T* C = buf + J.ctab;
-    for (int o = warp; o < n; o += nwarps) {
-      T acc = 0;
-      if (!J.inverse) {
-        const T* Crow = C + (long long)o * n;
-        for (int j = 0; j < n; ++j) acc += Crow[j] * tile[j * 33 + lane];
-      } else {
-        for (int k = 0; k < n; ++k) acc += C[(long long)k * n + o] * tile[k * 33 + lane];
-      }
-      if (act) buf[J.out + (long long)o * J.batch + col] = acc * scale;
-    }
-    __syncthreads();
-  }
-}
+// ---------------------------------------------------------------------------
+// Modal update
+// ---------------------------------------------------------------------------
 
 template <typename T>
 struct ModalArgs {
   T* buf;
   const DctDev* dct;
-  const int4* tiles;       // {air partition, kx chunk, ky block, kz block}
+  const int4* tiles;        // {air partition, kx tile, ky tile, kz tile}
   int ntiles;
   const PointDev* srcs;
   const PointDev* recs;
-  const float* series;     // [n_sources][max_steps]
+  const float* series;      // [n_sources][max_steps]
   long long max_steps;
-  const long long* tcount; // steps completed before the current graph launch
-  int tstep;               // step offset inside the launch
+  const long long* tcount;  // steps completed before the current launch sequence
+  int tstep;                // step offset inside the sequence
   int par;
 };
 
-template <typename T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
+// Shared memory of the modal kernel, in elements of T.
+constexpr int kModalRySlot = 3 * 1024;  // [3 n][rpc * kxt = 1024]
+constexpr int kModalSmemElems = 2 * kModalRySlot + 2 * kMaxPointsPerPart * 128 + 8 * kMaxPointsPerPart;
 
-// One warp per tile of 32 kx x kModalTY ky x TZ kz modes.  REF selects the
-// reference's arithmetic (tables cos, w^2) over the accurate one (1-cos, psi).
+// One block (8 warps) per tile of kxt kx x rpc ky x TZ kz modes; a thread
+// owns 4 consecutive kx of one ky row.  Per mode it reads M(t-1), M(t-2)
+// and the two tables and writes M(t) (all 128-bit, row pitch wp), expands
+// the face transforms into the force mode F, and contracts M(t) onto the face
+// rows: along kx by a shuffle butterfly (partial per kx tile), along ky
+// through shared memory (partial per ky tile), along kz in registers
+// (partial per kz tile).  REF selects the reference's arithmetic.
 template <typename T, bool REF>
-__global__ void __launch_bounds__(128) modal_kernel(ModalArgs<T> a) {
-  constexpr int TY = kModalTY;
-  const int lane = threadIdx.x & 31;
-  const int tile_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (tile_id >= a.ntiles) return;
-  const int4 tl = a.tiles[tile_id];
-  const DctDev& D = a.dct[tl.x];
-  const int w = D.w, h = D.h, d = D.d;
-  const int kx = tl.y * 32 + lane;
-  const bool act = kx < w;
-  const int kxc = act ? kx : w - 1;
-  const int px = kx & 1;
+__global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* ry_s = reinterpret_cast<T*>(smem_raw);
+  T* cws = ry_s + 2 * kModalRySlot;                  // [kMaxPointsPerPart][128]
+  T* cwr = cws + kMaxPointsPerPart * 128;            // [kMaxPointsPerPart][128]
+  T* red = cwr + kMaxPointsPerPart * 128;            // [8 warps][kMaxPointsPerPart]
+  __shared__ int pts_y[2][kMaxPointsPerPart], pts_z[2][kMaxPointsPerPart];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   T* __restrict__ buf = a.buf;
-  const T* Cw = buf + D.cw;
-  const T* Ch = buf + D.ch;
-  const T* Cd = buf + D.cd;
-  // REDFT10 row kx for the expansion; REDFT01 weights (k = 0 halved) for the contraction
-  T cx[3], cxi[3];
-#pragma unroll
-  for (int n = 0; n < 3; ++n) {
-    cx[n] = Cw[(long long)kxc * w + n];
-    cxi[n] = kx == 0 ? (T)0.5 * cx[n] : cx[n];
-  }
-  const int ky0 = tl.z * TY;
-  const int nky = min(TY, h - ky0);
-  const int kz0 = tl.w * D.TZ;
-  const int kz1 = min(kz0 + D.TZ, d);
-  const T* Mcur = buf + D.M[a.par ^ 1];   // M(t-1)
-  T* Mout = buf + D.M[a.par];             // holds M(t-2); receives M(t)
-  const T* tabA = buf + D.tabA;
-  const T* tabB = buf + D.tabB;
-  const T* PX = buf + D.PX;
-  const T* PY = buf + D.PY;
-  const T* PZ = buf + D.PZ;
-  const long long planeZ = (long long)h * w, planeY = (long long)d * w, planeX = (long long)d * h;
-
-  T pz[TY][2][3], rz[TY][2][3];
-#pragma unroll
-  for (int i = 0; i < TY; ++i)
-#pragma unroll
-    for (int pm = 0; pm < 2; ++pm)
-#pragma unroll
-      for (int n = 0; n < 3; ++n) {
-        pz[i][pm][n] = (i < nky && act) ? PZ[(pm * 3 + n) * planeZ + (long long)(ky0 + i) * w + kx] : (T)0;
-        rz[i][pm][n] = 0;
-      }
-
   const long long t = *a.tcount + a.tstep;
-  T sx[kMaxPointsPerPart];
-  int sy[kMaxPointsPerPart], sz[kMaxPointsPerPart];
-  const int nsrc = D.nsrc;
-#pragma unroll
-  for (int s = 0; s < kMaxPointsPerPart; ++s) {
-    sx[s] = 0; sy[s] = 0; sz[s] = 0;
-    if (s < nsrc) {
+
+  for (int tile_id = blockIdx.x; tile_id < a.ntiles; tile_id += gridDim.x) {
+    const int4 tl = a.tiles[tile_id];
+    const DctDev& D = a.dct[tl.x];
+    const int w = D.w, h = D.h, d = D.d, wp = D.wp, G = D.G, KXT = D.kxt, RPC = D.rpc;
+    const int rs = warp * (32 / G) + lane / G;   // row slot in the tile
+    const int li = lane % G;
+    const int kl0 = 4 * li;
+    const int kx0 = tl.y * KXT + kl0;
+    const int ky0 = tl.z * RPC;
+    const int ky = ky0 + rs;
+    const bool rowok = ky < h;
+    const bool lanok = rowok && kx0 < wp;
+    const int kz0 = tl.w * D.TZ, kz1 = min(kz0 + D.TZ, d);
+    const int nsrc = D.nsrc, nrec = D.nrec;
+    const T* Cw = buf + D.cw;
+    const T* Ch = buf + D.ch;
+    const T* Cd = buf + D.cd;
+    const T* Cwi = Cw + (long long)w * w;
+    const T* Chi = Ch + (long long)h * h;
+    const T* Cdi = Cd + (long long)d * d;
+
+    __syncthreads();  // the previous tile is done with shared memory
+    for (int i = tid; i < nsrc * KXT; i += kModalThreads) {
+      const int s = i / KXT, kl = i - s * KXT, kx = tl.y * KXT + kl;
       const PointDev q = a.srcs[D.src0 + s];
       const float v = (t < a.max_steps) ? a.series[(long long)q.slot * a.max_steps + t] : 0.0f;
-      sx[s] = (T)D.sf * (T)v * Cw[(long long)kxc * w + q.x];
-      sy[s] = q.y; sz[s] = q.z;
+      cws[s * 128 + kl] = kx < w ? (T)D.sf * (T)v * Cw[(long long)kx * w + q.x] : (T)0;
+      if (kl == 0) { pts_y[0][s] = q.y; pts_z[0][s] = q.z; }
     }
-  }
-  T rxc[kMaxPointsPerPart], racc[kMaxPointsPerPart];
-  int ry_[kMaxPointsPerPart], rz_[kMaxPointsPerPart];
-  const int nrec = D.nrec;
-#pragma unroll
-  for (int r = 0; r < kMaxPointsPerPart; ++r) {
-    rxc[r] = 0; racc[r] = 0; ry_[r] = 0; rz_[r] = 0;
-    if (r < nrec) {
+    for (int i = tid; i < nrec * KXT; i += kModalThreads) {
+      const int r = i / KXT, kl = i - r * KXT, kx = tl.y * KXT + kl;
       const PointDev q = a.recs[D.rec0 + r];
-      rxc[r] = act ? (kx == 0 ? (T)0.5 : (T)1) * Cw[(long long)kxc * w + q.x] : (T)0;
-      ry_[r] = q.y; rz_[r] = q.z;
+      cwr[r * 128 + kl] = kx < w ? Cwi[(long long)kx * w + q.x] : (T)0;
+      if (kl == 0) { pts_y[1][r] = q.y; pts_z[1][r] = q.z; }
     }
-  }
+    __syncthreads();
 
-  for (int kz = kz0; kz < kz1; ++kz) {
-    const int pzr = kz & 1;
-    T cz[3], czi[3], py[2][3], ry[2][3];
+    T cx[4][3];
+    bool act[4];
 #pragma unroll
-    for (int n = 0; n < 3; ++n) {
-      cz[n] = Cd[(long long)kz * d + n];
-      czi[n] = kz == 0 ? (T)0.5 * cz[n] : cz[n];
+    for (int e = 0; e < 4; ++e) {
+      act[e] = rowok && (kx0 + e < w);
+      const int kxe = min(kx0 + e, w - 1);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) cx[e][n] = Cw[(long long)kxe * w + n];
     }
+    const T wx0 = (kx0 == 0) ? (T)0.5 : (T)1;   // REDFT01 halves the k = 0 row
+    const int kyc = rowok ? ky : 0;
+    T cy[3];
+#pragma unroll
+    for (int n = 0; n < 3; ++n) cy[n] = Ch[(long long)kyc * h + n];
+    const T wy = (ky == 0) ? (T)0.5 : (T)1;
+    const int pyr = ky & 1;
+    const long long planeX = (long long)d * h, planeY = (long long)d * wp, planeZ = (long long)h * wp;
+    const T* PX = buf + D.PX;
+    const T* PYr = buf + D.PY + pyr * 3 * planeY;
+    T pz[2][3][4], rz[2][3][4];
 #pragma unroll
     for (int pm = 0; pm < 2; ++pm)
 #pragma unroll
       for (int n = 0; n < 3; ++n) {
-        py[pm][n] = act ? PY[(pm * 3 + n) * planeY + (long long)kz * w + kx] : (T)0;
-        ry[pm][n] = 0;
+        if (lanok) {
+          load4(buf + D.PZ + (pm * 3 + n) * planeZ + (long long)ky * wp + kx0, pz[pm][n]);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) pz[pm][n][e] = 0;
+        }
+#pragma unroll
+        for (int e = 0; e < 4; ++e) rz[pm][n][e] = 0;
       }
+    T racc[kMaxPointsPerPart];
 #pragma unroll
-    for (int i = 0; i < TY; ++i) {
-      if (i < nky) {
-        const int ky = ky0 + i;
-        const int pyr = ky & 1;
-        T cy[3];
+    for (int r = 0; r < kMaxPointsPerPart; ++r) racc[r] = 0;
+    const T* Mcur = buf + D.M[a.par ^ 1];   // M(t-1)
+    T* Mout = buf + D.M[a.par];             // holds M(t-2); receives M(t)
+    const T* tabA = buf + D.tabA;
+    const T* tabB = buf + D.tabB;
+    const T damping = (T)D.damping;
+
+    auto body = [&](auto parity, int kz) {
+      constexpr int PZ = decltype(parity)::value;  // kz & 1 (kz0 is even)
+      T cz[3];
 #pragma unroll
-        for (int n = 0; n < 3; ++n) cy[n] = Ch[(long long)ky * h + n];
-        T F = 0;
+      for (int n = 0; n < 3; ++n) cz[n] = Cd[(long long)kz * d + n];
+      const T wz = (kz == 0) ? (T)0.5 : (T)1;
+      T px[2][3];
 #pragma unroll
-        for (int n = 0; n < 3; ++n) F += cx[n] * PX[(px * 3 + n) * planeX + (long long)kz * h + ky];
+      for (int pm = 0; pm < 2; ++pm)
 #pragma unroll
-        for (int n = 0; n < 3; ++n) F += cy[n] * py[pyr][n];
+        for (int n = 0; n < 3; ++n) px[pm][n] = rowok ? PX[(pm * 3 + n) * planeX + (long long)kz * h + ky] : (T)0;
+      T py[3][4];
+      T m[4], mp[4], ta[4], tb[4];
+      const long long row = ((long long)kz * h + ky) * wp + kx0;
+      if (lanok) {
 #pragma unroll
-        for (int n = 0; n < 3; ++n) F += cz[n] * pz[i][pzr][n];
+        for (int n = 0; n < 3; ++n) load4(PYr + n * planeY + (long long)kz * wp + kx0, py[n]);
+        load4(Mcur + row, m);
+        load4(Mout + row, mp);
+        load4(tabA + row, ta);
+        load4(tabB + row, tb);
+      } else {
 #pragma unroll
-        for (int s = 0; s < kMaxPointsPerPart; ++s)
-          if (s < nsrc) F += sx[s] * (Ch[(long long)ky * h + sy[s]] * Cd[(long long)kz * d + sz[s]]);
-        const long long idx = ((long long)kz * h + ky) * w + kxc;
-        T Mn = 0;
-        if (act) {
-          const T m = Mcur[idx], mp = Mout[idx], ta = tabA[idx], tb = tabB[idx];
-          if (REF)  // dct_partition.cpp:68: a (2 M cwt - M_prev + (2 F / w2) (1 - cwt))
-            Mn = (T)D.damping * ((T)2 * m * ta - mp + ((T)2 * F / tb) * ((T)1 - ta));
-          else      // same recurrence with ta = 1 - cwt and tb = 2 (1 - cwt) / w2
-            Mn = (T)D.damping * (((T)2 * m - mp) - (T)2 * ta * m + tb * F);
-          Mout[idx] = Mn;
+        for (int e = 0; e < 4; ++e) {
+          py[0][e] = py[1][e] = py[2][e] = 0;
+          m[e] = mp[e] = ta[e] = 0;
+          tb[e] = 1;
         }
-        const T wy = ky == 0 ? (T)0.5 : (T)1;
-#pragma unroll
-        for (int n = 0; n < 3; ++n) {
-          rz[i][pzr][n] += czi[n] * Mn;
-          ry[pyr][n] += wy * cy[n] * Mn;
-        }
-        T v[6];
-#pragma unroll
-        for (int n = 0; n < 3; ++n) {
-          const T c = cxi[n] * Mn;
-          v[n] = px ? (T)0 : c;
-          v[3 + n] = px ? c : (T)0;
-        }
-#pragma unroll
-        for (int q = 0; q < 6; ++q) v[q] = warp_sum(v[q]);
-        if (lane < 6) {
-          T val = v[0];
-#pragma unroll
-          for (int q = 1; q < 6; ++q) if (lane == q) val = v[q];
-          // RX[bx][pm][n][kz][ky], lane = pm*3 + n
-          buf[D.RX + ((long long)tl.y * 6 + lane) * planeX + (long long)kz * h + ky] = val;
-        }
-#pragma unroll
-        for (int r = 0; r < kMaxPointsPerPart; ++r)
-          if (r < nrec)
-            racc[r] += rxc[r] * (wy * Ch[(long long)ky * h + ry_[r]] * ((kz == 0 ? (T)0.5 : (T)1) * Cd[(long long)kz * d + rz_[r]])) * Mn;
       }
+      T F[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        T f = 0;
+#pragma unroll
+        for (int n = 0; n < 3; ++n) f += cx[e][n] * px[e & 1][n];
+#pragma unroll
+        for (int n = 0; n < 3; ++n) f += cy[n] * py[n][e];
+#pragma unroll
+        for (int n = 0; n < 3; ++n) f += cz[n] * pz[PZ][n][e];
+        F[e] = f;
+      }
+      for (int s = 0; s < nsrc; ++s) {
+        const T coef = Ch[(long long)kyc * h + pts_y[0][s]] * Cd[(long long)kz * d + pts_z[0][s]];
+        T c[4];
+        load4(cws + s * 128 + kl0, c);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) F[e] += c[e] * coef;
+      }
+      T Mn[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        T v;
+        if (REF)  // dct_partition.cpp:68: a (2 M cwt - M_prev + (2 F / w2) (1 - cwt))
+          v = damping * ((T)2 * m[e] * ta[e] - mp[e] + ((T)2 * F[e] / tb[e]) * ((T)1 - ta[e]));
+        else      // the same recurrence with ta = 1 - cwt, tb = 2 (1 - cwt) / w2
+          v = damping * (((T)2 * m[e] - mp[e]) - (T)2 * ta[e] * m[e] + tb[e] * F[e]);
+        Mn[e] = act[e] ? v : (T)0;
+      }
+      if (lanok) store4(Mout + row, Mn);
+      // contraction along kz (registers) and ky (shared memory, reduced below)
+      T* slot = ry_s + PZ * kModalRySlot;
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        T ry[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          rz[PZ][n][e] += wz * cz[n] * Mn[e];
+          ry[e] = wy * cy[n] * Mn[e];
+        }
+        store4(slot + n * 1024 + rs * KXT + kl0, ry);
+      }
+      // contraction along kx: even / odd kx sums, butterfly over the row's lanes
+      T v[6];
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        v[n] = wx0 * cx[0][n] * Mn[0] + cx[2][n] * Mn[2];
+        v[3 + n] = cx[1][n] * Mn[1] + cx[3][n] * Mn[3];
+      }
+      for (int o = G >> 1; o > 0; o >>= 1)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+      if (rowok && li < 6) {
+        T val = v[0];
+#pragma unroll
+        for (int q = 1; q < 6; ++q)
+          if (li == q) val = v[q];
+        buf[D.RX + ((long long)tl.y * 6 + li) * planeX + (long long)kz * h + ky] = val;
+      }
+      for (int r = 0; r < nrec; ++r) {
+        const T coef = Chi[(long long)kyc * h + pts_y[1][r]] * Cdi[(long long)kz * d + pts_z[1][r]];
+        T c[4];
+        load4(cwr + r * 128 + kl0, c);
+        racc[r] += coef * (c[0] * Mn[0] + c[1] * Mn[1] + c[2] * Mn[2] + c[3] * Mn[3]);
+      }
+      __syncthreads();
+      // ky contraction of this kz: sum the tile's rows of matching parity
+      for (int o = tid; o < 6 * KXT; o += kModalThreads) {
+        const int pm = o / (3 * KXT);
+        const int rem = o - pm * 3 * KXT;
+        const int n = rem / KXT, kl = rem - n * KXT;
+        const int kx = tl.y * KXT + kl;
+        if (kx >= wp) continue;
+        T s = 0;
+        for (int r = ((ky0 & 1) == pm) ? 0 : 1; r < RPC && ky0 + r < h; r += 2) s += slot[n * 1024 + r * KXT + kl];
+        buf[D.RY + ((long long)tl.z * 6 + pm * 3 + n) * planeY + (long long)kz * wp + kx] = s;
+      }
+    };
+
+    for (int kz = kz0; kz < kz1; kz += 2) {
+      body(std::integral_constant<int, 0>{}, kz);
+      if (kz + 1 < kz1) body(std::integral_constant<int, 1>{}, kz + 1);
     }
-    if (act) {
+    if (lanok) {
 #pragma unroll
       for (int pm = 0; pm < 2; ++pm)
 #pragma unroll
         for (int n = 0; n < 3; ++n)
-          buf[D.RY + ((long long)tl.z * 6 + pm * 3 + n) * planeY + (long long)kz * w + kx] = ry[pm][n];
+          store4(buf + D.RZ + ((long long)tl.w * 6 + pm * 3 + n) * planeZ + (long long)ky * wp + kx0, rz[pm][n]);
     }
-  }
-  if (act) {
+    if (nrec > 0) {
 #pragma unroll
-    for (int i = 0; i < TY; ++i)
-      if (i < nky)
-#pragma unroll
-        for (int pm = 0; pm < 2; ++pm)
-#pragma unroll
-          for (int n = 0; n < 3; ++n)
-            buf[D.RZ + ((long long)tl.w * 6 + pm * 3 + n) * planeZ + (long long)(ky0 + i) * w + kx] = rz[i][pm][n];
-  }
-  if (nrec > 0) {
-    const int local = (tl.y * D.nby + tl.z) * D.nbz + tl.w;
-#pragma unroll
-    for (int r = 0; r < kMaxPointsPerPart; ++r) {
-      if (r < nrec) {
-        const T s = warp_sum(racc[r]);
-        if (lane == 0) buf[D.recpart + (long long)local * nrec + r] = s;
+      for (int r = 0; r < kMaxPointsPerPart; ++r) {
+        if (r < nrec) {
+          const T s = warp_sum(racc[r]);
+          if (lane == 0) red[warp * kMaxPointsPerPart + r] = s;
+        }
+      }
+      __syncthreads();
+      if (tid < nrec) {
+        T s = 0;
+        for (int k = 0; k < kModalThreads / 32; ++k) s += red[k * kMaxPointsPerPart + tid];
+        const int local = (tl.y * D.nby + tl.z) * D.nbz + tl.w;
+        buf[D.recpart + (long long)local * nrec + tid] = s;
       }
     }
   }
@@ -345,85 +444,106 @@ __global__ void recorder_kernel(const T* __restrict__ buf, const DctDev* __restr
   if (lane == 0 && t < max_steps) hist[t * nrec_total + q.slot] = (double)(s * (T)D.si);
 }
 
+// ---------------------------------------------------------------------------
+// PML
+// ---------------------------------------------------------------------------
+
 template <typename T>
 struct PmlArgs {
   T* buf;
   const PmlDev* pml;
-  const long long* start;  // first cell of each slab (prefix)
-  int npml;
-  long long total;
+  const int4* blocks;   // {slab, a0, b0}: 8 x 32 plane tiles
+  int nblocks;
   int par;
   T dt, dh, c0;
 };
 
 // Grote-Sim PML (pml_partition.cpp:113-200) in slab coordinates: layer l
-// along the normal, (a, b) in the plane.  Only the normal damping zeta_n is
-// non-zero in a slab, so zeta_a = zeta_b = 0 in the reference's formulas.
+// along the normal, (a, b) in the plane; outside the slab every field reads
+// zero (the reference's sentinel cell).  Only the normal damping zeta_n is
+// non-zero in a slab (zeta_a = zeta_b = 0 in the reference's formulas).  A
+// thread owns one (a, b) column and keeps p and phi_n of all layers in
+// registers; in-plane neighbours come through L1.
 template <typename T>
-__global__ void __launch_bounds__(256) pml_kernel(PmlArgs<T> a) {
+__global__ void __launch_bounds__(256, 2) pml_kernel(PmlArgs<T> a) {
   const T c7[7] = {2, -27, 270, -490, 270, -27, 2};
   const T c5[5] = {1, -8, 0, 8, -1};
-  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < a.total;
-       g += (long long)gridDim.x * blockDim.x) {
-    int lo = 0, hi = a.npml - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (a.start[mid] <= g) lo = mid; else hi = mid - 1;
-    }
-    const PmlDev& P = a.pml[lo];
-    const long long cell = g - a.start[lo];
-    const int AB = P.A * P.B;
-    const int l = (int)(cell / AB);
-    const int rem = (int)(cell - (long long)l * AB);
-    const int ia = rem / P.B, ib = rem - ia * P.B;
+  for (int bi = blockIdx.x; bi < a.nblocks; bi += gridDim.x) {
+    const int4 blk = a.blocks[bi];
+    const PmlDev& P = a.pml[blk.x];
+    const int ia = blk.y + (threadIdx.x >> 5), ib = blk.z + (threadIdx.x & 31);
+    if (ia >= P.A || ib >= P.B) continue;
+    const int L = P.L, A = P.A, B = P.B;
+    const long long lstride = (long long)A * B;
+    const long long col = (long long)ia * B + ib;
     const T* p = a.buf + P.p[a.par ^ 1];   // p(t-1)
     T* pn = a.buf + P.p[a.par];            // p(t-2) -> p(t)
     const T* fn = a.buf + P.phn[a.par ^ 1];
     const T* fa = a.buf + P.pha[a.par ^ 1];
     const T* fb = a.buf + P.phb[a.par ^ 1];
-    auto at = [&](const T* arr, int l2, int a2, int b2) -> T {
-      if (l2 < 0 || l2 >= P.L || a2 < 0 || a2 >= P.A || b2 < 0 || b2 >= P.B) return (T)0;
-      return arr[((long long)l2 * P.A + a2) * P.B + b2];
-    };
-    T ln = 0, la = 0, lb = 0;
+    T* fn_o = a.buf + P.phn[a.par];
+    T* fa_o = a.buf + P.pha[a.par];
+    T* fb_o = a.buf + P.phb[a.par];
+    const T* zeta = a.buf + P.zeta;
+    const T* force = a.buf + P.force;
+    T pc[kMaxPmlLayers + 6], fc[kMaxPmlLayers + 4];
 #pragma unroll
-    for (int m = 0; m < 7; ++m) {
-      ln += c7[m] * at(p, l + m - 3, ia, ib);
-      la += c7[m] * at(p, l, ia + m - 3, ib);
-      lb += c7[m] * at(p, l, ia, ib + m - 3);
+    for (int l = 0; l < kMaxPmlLayers + 6; ++l) {
+      const int ll = l - 3;
+      pc[l] = (ll >= 0 && ll < L) ? p[ll * lstride + col] : (T)0;
     }
-    const T d180 = (T)180 * a.dh * a.dh;
-    ln /= d180; la /= d180; lb /= d180;
-    const T zn = a.buf[P.zeta + l];
-    const long long I = cell;
-    const T pc = p[I], po = pn[I];
-    const T t1 = 2 * pc;
-    const T t2 = -po;
-    const T t3 = a.c0 * a.c0 * (ln + la + lb);
-    const T t4 = -zn * (pc - po) / a.dt;
-    T gn = 0, ga = 0, gb = 0, un = 0, ua = 0, ub = 0;
 #pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      gn += c5[m] * at(fn, l + m - 2, ia, ib);
-      ga += c5[m] * at(fa, l, ia + m - 2, ib);
-      gb += c5[m] * at(fb, l, ia, ib + m - 2);
-      un += c5[m] * at(p, l + m - 2, ia, ib);
-      ua += c5[m] * at(p, l, ia + m - 2, ib);
-      ub += c5[m] * at(p, l, ia, ib + m - 2);
+    for (int l = 0; l < kMaxPmlLayers + 4; ++l) {
+      const int ll = l - 2;
+      fc[l] = (ll >= 0 && ll < L) ? fn[ll * lstride + col] : (T)0;
     }
-    const T d12 = (T)12 * a.dh;
-    gn /= d12; ga /= d12; gb /= d12;
-    un /= d12; ua /= d12; ub /= d12;
-    const T t6 = gn + ga + gb;
-    const int sl = l - P.strip0;
-    const T f = (sl >= 0 && sl < 3) ? a.buf[P.force + ((long long)sl * P.A + ia) * P.B + ib] : (T)0;
-    pn[I] = t1 + t2 + a.dt * a.dt * (t3 + t4 + t6 + f);
-    const T fnc = fn[I], fac = fa[I], fbc = fb[I];
-    a.buf[P.phn[a.par] + I] = fnc - a.dt * zn * fnc + a.dt * (-zn) * un;
-    a.buf[P.pha[a.par] + I] = fac + a.dt * zn * ua;
-    a.buf[P.phb[a.par] + I] = fbc + a.dt * zn * ub;
+    const T d180 = (T)180 * a.dh * a.dh, d12 = (T)12 * a.dh;
+#pragma unroll
+    for (int l = 0; l < kMaxPmlLayers; ++l) {
+      if (l >= L) break;
+      const long long I = l * lstride + col;
+      const T* pl = p + l * lstride;
+      T ln = 0, la = 0, lb = 0, un = 0, ua = 0, ub = 0, gn = 0, ga = 0, gb = 0;
+#pragma unroll
+      for (int m = 0; m < 7; ++m) {
+        const int aa = ia + m - 3, bb = ib + m - 3;
+        ln += c7[m] * pc[l + m];
+        la += c7[m] * ((aa >= 0 && aa < A) ? pl[(long long)aa * B + ib] : (T)0);
+        lb += c7[m] * ((bb >= 0 && bb < B) ? pl[(long long)ia * B + bb] : (T)0);
+      }
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const int aa = ia + m - 2, bb = ib + m - 2;
+        const T pa = (aa >= 0 && aa < A) ? pl[(long long)aa * B + ib] : (T)0;
+        const T pb = (bb >= 0 && bb < B) ? pl[(long long)ia * B + bb] : (T)0;
+        un += c5[m] * pc[l + m + 1];
+        ua += c5[m] * pa;
+        ub += c5[m] * pb;
+        gn += c5[m] * fc[l + m];
+        ga += c5[m] * ((aa >= 0 && aa < A) ? fa[l * lstride + (long long)aa * B + ib] : (T)0);
+        gb += c5[m] * ((bb >= 0 && bb < B) ? fb[l * lstride + (long long)ia * B + bb] : (T)0);
+      }
+      ln /= d180; la /= d180; lb /= d180;
+      un /= d12; ua /= d12; ub /= d12;
+      gn /= d12; ga /= d12; gb /= d12;
+      const T zn = zeta[l];
+      const T pcur = pc[l + 3], pold = pn[I];
+      const int sl = l - P.strip0;
+      const T f = (sl >= 0 && sl < 3) ? force[sl * lstride + col] : (T)0;
+      const T t3 = a.c0 * a.c0 * (ln + la + lb);
+      const T t4 = -zn * (pcur - pold) / a.dt;
+      pn[I] = (T)2 * pcur - pold + a.dt * a.dt * (t3 + t4 + (gn + ga + gb) + f);
+      const T fnc = fc[l + 2];
+      fn_o[I] = fnc - a.dt * zn * fnc + a.dt * (-zn) * un;
+      fa_o[I] = fa[I] + a.dt * zn * ua;
+      fb_o[I] = fb[I] + a.dt * zn * ub;
+    }
   }
 }
+
+// ---------------------------------------------------------------------------
+// Interfaces
+// ---------------------------------------------------------------------------
 
 template <typename T>
 struct IfaceArgs {
@@ -445,8 +565,8 @@ __device__ __forceinline__ T side_pressure(const IfaceArgs<T>& a, int type, cons
     const DctDev& D = a.dct[s.idx];
     const int layer = face_layer(c, s.ext);
     if (type == 0) return a.buf[D.pX + ((long long)layer * D.d + v) * D.h + u];
-    if (type == 1) return a.buf[D.pY + ((long long)layer * D.d + v) * D.w + u];
-    return a.buf[D.pZ + ((long long)layer * D.h + v) * D.w + u];
+    if (type == 1) return a.buf[D.pY + ((long long)layer * D.d + v) * D.wp + u];
+    return a.buf[D.pZ + ((long long)layer * D.h + v) * D.wp + u];
   }
   const PmlDev& P = a.pml[s.idx];
   return a.buf[P.p[a.par] + ((long long)c * P.A + v) * P.B + u];
@@ -525,35 +645,35 @@ static __global__ void advance_time_kernel(long long* tcount, int n) {
 
 // ---- setup kernels (FP64 arithmetic) ----
 
-// Per extent n, three n*n tables: C[k][j] = 2 cos(pi (j + 1/2) k / n) (the
-// REDFT10 matrix), its transpose, and the REDFT01 matrix Ci[k][j] = C[k][j]
-// with row k = 0 halved (REDFT01 weights X_0 by 1, the others by 2).
+// Per extent n, two n*n tables: C[k][j] = 2 cos(pi (j + 1/2) k / n) (the
+// REDFT10 matrix) and the REDFT01 matrix Ci[k][j] = C[k][j] with row k = 0
+// halved (REDFT01 weights X_0 by 1, the others by 2).
 template <typename T>
 __global__ void cos_table_kernel(T* buf, long long off, int n) {
   const long long nn = (long long)n * n;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(i / n), j = (int)(i - (long long)k * n);
-    // argument reduced exactly in integers
-    const long long q = ((long long)(2 * j + 1) * k) % (4LL * n);
+    const long long q = ((long long)(2 * j + 1) * k) % (4LL * n);  // argument reduced exactly in integers
     const double v = 2.0 * cospi((double)q / (2.0 * n));
-    buf[off + (long long)k * n + j] = (T)v;
-    buf[off + nn + (long long)j * n + k] = (T)v;
-    buf[off + 2 * nn + (long long)k * n + j] = (T)(k == 0 ? 0.5 * v : v);
+    buf[off + i] = (T)v;
+    buf[off + nn + i] = (T)(k == 0 ? 0.5 * v : v);
   }
 }
 
 // Accurate-arithmetic tables: tabA = 1 - cos(w dt) = 2 sin^2(w dt / 2),
-// tabB = 2 (1 - cos(w dt)) / w^2, in FP64 then rounded to T.
+// tabB = 2 (1 - cos(w dt)) / w^2, in FP64 then rounded to T; [d][h][wp],
+// padding columns zero.
 template <typename T>
-__global__ void modal_table_kernel(T* buf, long long tabA, long long tabB, int w, int h, int d, double dh, double dt,
-                                   double c0) {
-  const long long N = (long long)w * h * d;
+__global__ void modal_table_kernel(T* buf, long long tabA, long long tabB, int w, int wp, int h, int d, double dh,
+                                   double dt, double c0) {
+  const long long N = (long long)wp * h * d;
   const double lx = w * dh, ly = h * dh, lz = d * dh;
   const double pi = 3.14159265358979323846;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
-    const int kx = (int)(i % w);
-    const int ky = (int)((i / w) % h);
-    const int kz = (int)(i / ((long long)w * h));
+    const int kx = (int)(i % wp);
+    const int ky = (int)((i / wp) % h);
+    const int kz = (int)(i / ((long long)wp * h));
+    if (kx >= w) { buf[tabA + i] = 0; buf[tabB + i] = 0; continue; }
     // 1-based mode numbers, as dct_partition.cpp:24-36
     const double ax = (kx + 1) / lx, ay = (ky + 1) / ly, az = (kz + 1) / lz;
     const double omega = c0 * pi * sqrt(az * az + ay * ay + ax * ax);

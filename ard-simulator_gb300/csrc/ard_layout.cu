@@ -84,15 +84,15 @@ void pml_profile(const Ctx* ctx, int type, int L, double scale, std::vector<doub
 // sqrt / cos; tabA = cos(w dt), tabB = w^2.
 template <typename R>
 int upload_reference_tables(Ctx* ctx, const DctDev& D) {
-  const long long N = (long long)D.w * D.h * D.d;
-  std::vector<R> a((size_t)N), b((size_t)N);
+  const long long N = (long long)D.wp * D.h * D.d;
+  std::vector<R> a((size_t)N, (R)0), b((size_t)N, (R)0);
   const R dh = (R)(float)ctx->dh, dt = (R)(float)ctx->dt, c0 = (R)(float)ctx->c0;
   const R lx2 = D.w * D.w * dh * dh, ly2 = D.h * D.h * dh * dh, lz2 = D.d * D.d * dh * dh;
   const R pi = (R)M_PI;
   for (int i = 1; i <= D.d; ++i)
     for (int j = 1; j <= D.h; ++j)
       for (int k = 1; k <= D.w; ++k) {
-        const long long idx = (long long)(i - 1) * D.h * D.w + (long long)(j - 1) * D.w + (k - 1);
+        const long long idx = ((long long)(i - 1) * D.h + (j - 1)) * D.wp + (k - 1);
         const R w = c0 * pi * std::sqrt(i * i / lz2 + j * j / ly2 + k * k / lx2);
         b[idx] = w * w;
         a[idx] = std::cos(w * dt);
@@ -125,14 +125,12 @@ int upload_pml_zeta(Ctx* ctx) {
 int zero_state(Ctx* ctx) {
   const size_t es = elem_size(ctx);
   for (const DctDev& D : ctx->dct) {
-    const long long N = (long long)D.w * D.h * D.d;
-    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.M[0] * es, 0, N * es, ctx->stream));
-    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.M[1] * es, 0, N * es, ctx->stream));
-    const long long faces = 6LL * ((long long)D.d * D.h + (long long)D.d * D.w + (long long)D.h * D.w);
-    // fX..fZ and pX..pZ are contiguous runs of `faces` elements each
-    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.fX * es, 0, (D.fZ - D.fX + 6LL * D.h * D.w) * es, ctx->stream));
-    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.pX * es, 0, (D.pZ - D.pX + 6LL * D.h * D.w) * es, ctx->stream));
-    (void)faces;
+    const long long Np = (long long)D.wp * D.h * D.d;
+    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.M[0] * es, 0, Np * es, ctx->stream));
+    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.M[1] * es, 0, Np * es, ctx->stream));
+    // fX..fZ and pX..pZ are contiguous runs
+    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.fX * es, 0, (D.fZ - D.fX + 6LL * D.h * D.wp) * es, ctx->stream));
+    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.pX * es, 0, (D.pZ - D.pX + 6LL * D.h * D.wp) * es, ctx->stream));
   }
   for (const PmlDev& P : ctx->pml) {
     for (int k = 0; k < 2; ++k) {
@@ -167,7 +165,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   auto cos_table = [&](int n) {
     auto it = cos_off.find(n);
     if (it != cos_off.end()) return it->second;
-    const long long o = pool.take(3LL * n * n);
+    const long long o = pool.take(2LL * n * n);
     cos_off[n] = o;
     ctx->maxn = std::max(ctx->maxn, n);
     return o;
@@ -189,10 +187,12 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
       if (p.kind == ARD_PART_DCT) {
         DctDev D{};
         D.w = p.width; D.h = p.height; D.d = p.depth;
+        D.wp = (D.w + 3) / 4 * 4;
         const long long N = (long long)D.w * D.h * D.d;
+        const long long Np = (long long)D.wp * D.h * D.d;
         ctx->n_air_cells += N;
-        D.M[0] = pool.take(N); D.M[1] = pool.take(N);
-        D.tabA = pool.take(N); D.tabB = pool.take(N);
+        D.M[0] = pool.take(Np); D.M[1] = pool.take(Np);
+        D.tabA = pool.take(Np); D.tabB = pool.take(Np);
         D.damping = sc.modal_damping;
         D.sf = 1.0 / (2.0 * std::sqrt(2.0 * (double)N));
         D.si = 1.0 / std::sqrt(2.0 * (double)N);
@@ -269,23 +269,35 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   }
 
   // ---- modal tiling ----
+  // A tile is 8 warps; a thread owns 4 consecutive kx.  G lanes cover one ky
+  // row (G = 8, 16 or 32, the smallest with 4 G >= min(wp, 128)), so a tile
+  // spans kxt = 4 G kx and rpc = 256 / G ky rows.  The kz extent TZ (even, or
+  // the whole depth) is chosen so that the tiles fill the GPU at least twice.
   long long col_tiles = 0;
-  for (const DctDev& D : ctx->dct) col_tiles += (long long)((D.w + 31) / 32) * ((D.h + kModalTY - 1) / kModalTY);
-  const long long target = (long long)ctx->num_sms * 12;
+  for (DctDev& D : ctx->dct) {
+    const int need = std::min(D.wp, 128) / 4;
+    D.G = need <= 8 ? 8 : (need <= 16 ? 16 : 32);
+    D.kxt = 4 * D.G;
+    D.rpc = kModalThreads / D.G;
+    D.nbx = (D.wp + D.kxt - 1) / D.kxt;
+    D.nby = (D.h + D.rpc - 1) / D.rpc;
+    col_tiles += (long long)D.nbx * D.nby;
+  }
+  const long long target = (long long)ctx->num_sms * 2;
   for (size_t k = 0; k < ctx->dct.size(); ++k) {
     DctDev& D = ctx->dct[k];
-    D.nbx = (D.w + 31) / 32;
-    D.nby = (D.h + kModalTY - 1) / kModalTY;
     long long nbz = col_tiles > 0 ? (target + col_tiles - 1) / col_tiles : 1;
-    nbz = std::max(1LL, std::min<long long>(nbz, D.d));
-    D.TZ = (int)((D.d + nbz - 1) / nbz);
+    nbz = std::max(1LL, std::min<long long>(nbz, D.d / 2));
+    int TZ = (int)((D.d + nbz - 1) / nbz);
+    if (TZ < D.d) TZ += TZ & 1;  // even, so every kz tile starts on an even plane
+    D.TZ = TZ;
     D.nbz = (D.d + D.TZ - 1) / D.TZ;
     D.tile0 = (int)ctx->tiles.size();
     for (int bx = 0; bx < D.nbx; ++bx)
       for (int by = 0; by < D.nby; ++by)
         for (int bz = 0; bz < D.nbz; ++bz) ctx->tiles.push_back(make_int4((int)k, bx, by, bz));
-    // face arrays
-    const long long FX = 6LL * D.d * D.h, FY = 6LL * D.d * D.w, FZ = 6LL * D.h * D.w;
+    // face arrays (Y and Z layers use the padded row pitch wp)
+    const long long FX = 6LL * D.d * D.h, FY = 6LL * D.d * D.wp, FZ = 6LL * D.h * D.wp;
     D.fX = pool.off; D.fY = D.fX + FX; D.fZ = D.fY + FY; pool.take(FX + FY + FZ);
     D.pX = pool.off; D.pY = D.pX + FX; D.pZ = D.pY + FY; pool.take(FX + FY + FZ);
     D.PX = pool.take(FX); D.PY = pool.take(FY); D.PZ = pool.take(FZ);
@@ -301,27 +313,33 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     ctx->scratch = pool.take(3 * maxN);
   }
 
-  // ---- PML arrays ----
-  for (PmlDev& P : ctx->pml) {
-    for (int k = 0; k < 2; ++k) {
-      P.p[k] = pool.take(P.n); P.phn[k] = pool.take(P.n); P.pha[k] = pool.take(P.n); P.phb[k] = pool.take(P.n);
+  // ---- PML arrays and 8 x 32 plane tiles ----
+  for (size_t k = 0; k < ctx->pml.size(); ++k) {
+    PmlDev& P = ctx->pml[k];
+    if (P.L > kMaxPmlLayers) {
+      ctx->err = "PML thicker than " + std::to_string(kMaxPmlLayers) + " layers";
+      return ARD_ERR_INVALID;
+    }
+    for (int q = 0; q < 2; ++q) {
+      P.p[q] = pool.take(P.n); P.phn[q] = pool.take(P.n); P.pha[q] = pool.take(P.n); P.phb[q] = pool.take(P.n);
     }
     P.force = pool.take(3LL * P.A * P.B);
     P.zeta = pool.take(P.L);
-    ctx->pml_start.push_back(ctx->n_pml_cells);
     ctx->n_pml_cells += P.n;
+    for (int a0 = 0; a0 < P.A; a0 += 8)
+      for (int b0 = 0; b0 < P.B; b0 += 32) ctx->pml_blocks.push_back(make_int4((int)k, a0, b0, 0));
   }
 
   // ---- interfaces + owner masks ----
   std::vector<std::vector<int>> owner(ctx->dct.size());
   auto shell_local = [&](int k, int x, int y, int z) {
     DctDev D = ctx->dct[k];
-    D.fX = 0; D.fY = 6LL * D.d * D.h; D.fZ = D.fY + 6LL * D.d * D.w;
+    D.fX = 0; D.fY = 6LL * D.d * D.h; D.fZ = D.fY + 6LL * D.d * D.wp;
     return shell_index(D, x, y, z);
   };
   for (size_t k = 0; k < ctx->dct.size(); ++k) {
     const DctDev& D = ctx->dct[k];
-    owner[k].assign(6LL * ((long long)D.d * D.h + (long long)D.d * D.w + (long long)D.h * D.w), -1);
+    owner[k].assign(6LL * ((long long)D.d * D.h + (long long)D.d * D.wp + (long long)D.h * D.wp), -1);
   }
   struct PendingIface { IfaceDev dev; int scene; };
   std::vector<PendingIface> pend;
@@ -447,40 +465,49 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     }
   }
 
-  // ---- transform jobs ----
+  // ---- transform jobs (GEMMs over the face layers) ----
+  auto add_job = [](JobList& list, XformJob j) {
+    const int Md = j.rows ? j.batch : j.n, Nd = j.rows ? j.n : j.batch;
+    j.tn = (Nd + 63) / 64;
+    j.ntiles = ((Md + 63) / 64) * j.tn;
+    list.add(j, j.ntiles);
+  };
   for (const DctDev& D : ctx->dct) {
-    struct Axis { long long f, p, P, R, tmp; int nU, nV; long long cU, cV; int nb; };
+    // layer [V][ld], transforms along U (fast) and V (slow)
+    struct Axis { long long f, p, P, R, tmp; int nU, nV, ld; long long cU, cV; int nb; };
     const Axis axes[3] = {
-        {D.fX, D.pX, D.PX, D.RX, D.tmpX, D.h, D.d, D.ch, D.cd, D.nbx},
-        {D.fY, D.pY, D.PY, D.RY, D.tmpY, D.w, D.d, D.cw, D.cd, D.nby},
-        {D.fZ, D.pZ, D.PZ, D.RZ, D.tmpZ, D.w, D.h, D.cw, D.ch, D.nbz},
+        {D.fX, D.pX, D.PX, D.RX, D.tmpX, D.h, D.d, D.h, D.ch, D.cd, D.nbx},
+        {D.fY, D.pY, D.PY, D.RY, D.tmpY, D.w, D.d, D.wp, D.cw, D.cd, D.nby},
+        {D.fZ, D.pZ, D.PZ, D.RZ, D.tmpZ, D.w, D.h, D.wp, D.cw, D.ch, D.nbz},
     };
     for (const Axis& a : axes) {
-      const long long VU = (long long)a.nU * a.nV;
+      const long long LS = (long long)a.nV * a.ld;  // layer stride
       for (int pm = 0; pm < 2; ++pm)
         for (int n = 0; n < 3; ++n) {
           XformJob j{};
-          j.in0 = a.f + n * VU; j.in1 = a.f + (5 - n) * VU; j.sgn = pm ? -1 : 1;
-          j.out = a.tmp + (pm * 3 + n) * VU; j.ctab = a.cU; j.n = a.nU; j.batch = a.nV;
-          j.nparts = 1; j.part_stride = 0; j.inverse = 0; j.scale = 1.0;
-          ctx->fwd1.add(j, a.nV);
+          j.in0 = a.f + n * LS; j.in1 = a.f + (5 - n) * LS; j.sgn = pm ? -1 : 1;
+          j.out = a.tmp + (pm * 3 + n) * LS; j.ctab = a.cU; j.n = a.nU; j.batch = a.nV; j.ld = a.ld;
+          j.nparts = 1; j.part_stride = 0; j.inverse = 0; j.rows = 1; j.scale = 1.0;
+          add_job(ctx->fwd1, j);
           XformJob k{};
-          k.in0 = a.tmp + (pm * 3 + n) * VU; k.in1 = -1; k.sgn = 1;
-          k.out = a.P + (pm * 3 + n) * VU; k.ctab = a.cV; k.n = a.nV; k.batch = a.nU;
-          k.nparts = 1; k.part_stride = 0; k.inverse = 0; k.scale = D.sf;
-          ctx->fwd2.add(k, (a.nU + 31) / 32);
+          k.in0 = a.tmp + (pm * 3 + n) * LS; k.in1 = -1; k.sgn = 1;
+          k.out = a.P + (pm * 3 + n) * LS; k.ctab = a.cV; k.n = a.nV; k.batch = a.nU; k.ld = a.ld;
+          k.nparts = 1; k.part_stride = 0; k.inverse = 0; k.rows = 0; k.scale = D.sf;
+          add_job(ctx->fwd2, k);
         }
       for (int L = 0; L < 6; ++L) {
         const int n = L < 3 ? L : 5 - L;
         XformJob j{};
-        j.in0 = a.R + (0 * 3 + n) * VU; j.in1 = a.R + (1 * 3 + n) * VU; j.sgn = L < 3 ? 1 : -1;
-        j.nparts = a.nb; j.part_stride = 6 * VU;
-        j.out = a.tmp + L * VU; j.ctab = a.cV + 2LL * a.nV * a.nV; j.n = a.nV; j.batch = a.nU; j.inverse = 1; j.scale = 1.0;
-        ctx->inv1.add(j, (a.nU + 31) / 32);
+        j.in0 = a.R + (0 * 3 + n) * LS; j.in1 = a.R + (1 * 3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
+        j.nparts = a.nb; j.part_stride = 6 * LS;
+        j.out = a.tmp + L * LS; j.ctab = a.cV + (long long)a.nV * a.nV; j.n = a.nV; j.batch = a.nU; j.ld = a.ld;
+        j.inverse = 1; j.rows = 0; j.scale = 1.0;
+        add_job(ctx->inv1, j);
         XformJob k{};
-        k.in0 = a.tmp + L * VU; k.in1 = -1; k.sgn = 1; k.nparts = 1; k.part_stride = 0;
-        k.out = a.p + L * VU; k.ctab = a.cU + 2LL * a.nU * a.nU; k.n = a.nU; k.batch = a.nV; k.inverse = 1; k.scale = D.si;
-        ctx->inv2.add(k, a.nV);
+        k.in0 = a.tmp + L * LS; k.in1 = -1; k.sgn = 1; k.nparts = 1; k.part_stride = 0;
+        k.out = a.p + L * LS; k.ctab = a.cU + (long long)a.nU * a.nU; k.n = a.nU; k.batch = a.nV; k.ld = a.ld;
+        k.inverse = 1; k.rows = 1; k.scale = D.si;
+        add_job(ctx->inv2, k);
       }
     }
   }
@@ -488,10 +515,6 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   // ---- device allocation ----
   const size_t es = elem_size(ctx);
   ctx->pool_elems = pool.off;
-  if (33LL * ctx->maxn * (long long)es > ctx->smem_optin) {
-    ctx->err = "partition extent " + std::to_string(ctx->maxn) + " too large for the shared-memory transform tile";
-    return ARD_ERR_INVALID;
-  }
   ARD_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   ARD_CUDA(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
   ARD_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
@@ -510,7 +533,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   if ((rc = up(&ctx->d_mask, ctx->masks))) return rc;
   if ((rc = up(&ctx->d_dct, ctx->dct))) return rc;
   if ((rc = up(&ctx->d_pml, ctx->pml))) return rc;
-  if ((rc = up(&ctx->d_pml_start, ctx->pml_start))) return rc;
+  if ((rc = up(&ctx->d_pml_blocks, ctx->pml_blocks))) return rc;
   if ((rc = up(&ctx->d_ifs, ctx->ifs))) return rc;
   if ((rc = up(&ctx->d_srcpts, ctx->srcpts))) return rc;
   if ((rc = up(&ctx->d_recpts, ctx->recpts))) return rc;
@@ -534,7 +557,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     ARD_CUDA(cudaGetLastError());
   }
   for (const DctDev& D : ctx->dct) {
-    const long long N = (long long)D.w * D.h * D.d;
+    const long long N = (long long)D.wp * D.h * D.d;
     if (ctx->arith == ARD_ARITH_REFERENCE) {
       ARD_CUDA(cudaStreamSynchronize(ctx->stream));
       int rc2 = ctx->prec == ARD_PREC_F64 ? upload_reference_tables<double>(ctx, D) : upload_reference_tables<float>(ctx, D);
@@ -543,11 +566,11 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     }
     const int blocks = (int)std::min<long long>((N + 255) / 256, 8192);
     if (ctx->prec == ARD_PREC_F64)
-      modal_table_kernel<double><<<blocks, 256, 0, ctx->stream>>>((double*)ctx->d_buf, D.tabA, D.tabB, D.w, D.h, D.d,
+      modal_table_kernel<double><<<blocks, 256, 0, ctx->stream>>>((double*)ctx->d_buf, D.tabA, D.tabB, D.w, D.wp, D.h, D.d,
                                                                    (double)(float)ctx->dh, (double)(float)ctx->dt,
                                                                    (double)(float)ctx->c0);
     else
-      modal_table_kernel<float><<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, D.tabA, D.tabB, D.w, D.h, D.d,
+      modal_table_kernel<float><<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, D.tabA, D.tabB, D.w, D.wp, D.h, D.d,
                                                                   (double)(float)ctx->dh, (double)(float)ctx->dt,
                                                                   (double)(float)ctx->c0);
     ARD_CUDA(cudaGetLastError());
@@ -556,14 +579,14 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   ARD_CUDA(cudaStreamSynchronize(ctx->stream));
   if ((rc = upload_pml_zeta(ctx))) return rc;
   if ((rc = zero_state(ctx))) return rc;
-  // transform kernels may need more than 48 KB of dynamic shared memory
-  const int cols_smem = (int)(33LL * ctx->maxn * es), rows_smem = (int)(8LL * ctx->maxn * es);
+  // the FP64 modal kernel needs more than 48 KB of dynamic shared memory
+  const int modal_smem = (int)(kModalSmemElems * es);
   if (ctx->prec == ARD_PREC_F64) {
-    ARD_CUDA(cudaFuncSetAttribute(xform_cols_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, cols_smem));
-    ARD_CUDA(cudaFuncSetAttribute(xform_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, rows_smem));
+    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
+    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
   } else {
-    ARD_CUDA(cudaFuncSetAttribute(xform_cols_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, cols_smem));
-    ARD_CUDA(cudaFuncSetAttribute(xform_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, rows_smem));
+    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
+    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
   }
   ARD_CUDA(cudaStreamSynchronize(ctx->stream));
   return ARD_OK;
@@ -571,7 +594,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
 
 void free_ctx_device(Ctx* ctx) {
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
-  void* ptrs[] = {ctx->d_buf, ctx->d_mask, ctx->d_dct, ctx->d_pml, ctx->d_pml_start, ctx->d_ifs, ctx->d_srcpts,
+  void* ptrs[] = {ctx->d_buf, ctx->d_mask, ctx->d_dct, ctx->d_pml, ctx->d_pml_blocks, ctx->d_ifs, ctx->d_srcpts,
                   ctx->d_recpts, ctx->d_tiles, ctx->d_fwd1, ctx->d_fwd2, ctx->d_inv1, ctx->d_inv2, ctx->d_series,
                   ctx->d_hist, ctx->d_t};
   for (void* p : ptrs)
@@ -584,56 +607,56 @@ void free_ctx_device(Ctx* ctx) {
   ctx->d_buf = nullptr;
 }
 
-// Dense 3D transform of one air partition between pool offsets `in` and
-// `out` through a scratch area, with the rows / cols kernels:
-// forward  out = scale * REDFT10 on each axis (matrix C)
-// inverse  out = scale * REDFT01 on each axis (matrix Ci^T)
+// Dense 3D transform of one air partition, unpadded [d][h][w], from pool
+// offset `in` to `out` through `scratch` (in == out allowed), with the GEMM
+// kernel: forward applies REDFT10 (matrix C) on each axis, inverse REDFT01
+// (matrix Ci^T); `scale` multiplies the result.
 template <typename T>
 int dense_transform(Ctx* ctx, const DctDev& D, long long in, long long out, long long scratch, bool inverse,
                     double scale) {
   T* buf = reinterpret_cast<T*>(ctx->d_buf);
   const long long plane = (long long)D.h * D.w;
-  XformJob base{};
-  base.in1 = -1; base.sgn = 1; base.nparts = 1; base.part_stride = 0; base.inverse = inverse ? 1 : 0;
-  // three passes: x (rows), y (cols per z-slice), z (cols over the plane)
+  auto table = [&](int n) {
+    for (auto& kv : ctx->cos_tables)
+      if (kv.first == n) return kv.second + (inverse ? (long long)n * n : 0);
+    return -1LL;
+  };
+  auto make = [&](long long i0, long long o0, int n, int batch, int ld, int rows, double sc) {
+    XformJob j{};
+    j.in0 = i0; j.in1 = -1; j.sgn = 1; j.nparts = 1; j.part_stride = 0;
+    j.out = o0; j.ctab = table(n); j.n = n; j.batch = batch; j.ld = ld;
+    j.inverse = inverse ? 1 : 0; j.rows = rows; j.scale = sc;
+    const int Md = rows ? batch : n, Nd = rows ? n : batch;
+    j.tn = (Nd + 63) / 64;
+    j.ntiles = ((Md + 63) / 64) * j.tn;
+    return j;
+  };
   JobList px, py, pz;
-  const long long a = in, b = scratch, c = out;
-  // forward order x, y, z; inverse order z, y, x (transposes commute per axis, order is free)
+  const long long b = scratch;
   {
-    XformJob j = base;
-    j.in0 = a; j.out = b;
-    for (auto& kv : ctx->cos_tables) if (kv.first == D.w) j.ctab = kv.second + (inverse ? 2LL * D.w * D.w : 0);
-    j.n = D.w; j.batch = D.d * D.h; j.scale = 1.0;
-    px.add(j, j.batch);
+    XformJob j = make(in, b, D.w, D.d * D.h, D.w, 1, 1.0);
+    px.add(j, j.ntiles);
   }
   for (int z = 0; z < D.d; ++z) {
-    XformJob j = base;
-    j.in0 = b + z * plane; j.out = c + z * plane;
-    for (auto& kv : ctx->cos_tables) if (kv.first == D.h) j.ctab = kv.second + (inverse ? 2LL * D.h * D.h : 0);
-    j.n = D.h; j.batch = D.w; j.scale = 1.0;
-    py.add(j, (D.w + 31) / 32);
+    XformJob j = make(b + z * plane, out + z * plane, D.h, D.w, D.w, 0, 1.0);
+    py.add(j, j.ntiles);
   }
   {
-    XformJob j = base;
-    j.in0 = c; j.out = b;
-    for (auto& kv : ctx->cos_tables) if (kv.first == D.d) j.ctab = kv.second + (inverse ? 2LL * D.d * D.d : 0);
-    j.n = D.d; j.batch = (int)plane; j.scale = scale;
-    pz.add(j, (int)((plane + 31) / 32));
+    XformJob j = make(out, b, D.d, (int)plane, (int)plane, 0, scale);
+    pz.add(j, j.ntiles);
   }
   XformJob *dx = nullptr, *dy = nullptr, *dz = nullptr;
-  ARD_CUDA(cudaMalloc(&dx, sizeof(XformJob) * px.jobs.size()));
+  ARD_CUDA(cudaMalloc(&dx, sizeof(XformJob)));
   ARD_CUDA(cudaMalloc(&dy, sizeof(XformJob) * py.jobs.size()));
-  ARD_CUDA(cudaMalloc(&dz, sizeof(XformJob) * pz.jobs.size()));
-  ARD_CUDA(cudaMemcpy(dx, px.jobs.data(), sizeof(XformJob) * px.jobs.size(), cudaMemcpyHostToDevice));
+  ARD_CUDA(cudaMalloc(&dz, sizeof(XformJob)));
+  ARD_CUDA(cudaMemcpy(dx, px.jobs.data(), sizeof(XformJob), cudaMemcpyHostToDevice));
   ARD_CUDA(cudaMemcpy(dy, py.jobs.data(), sizeof(XformJob) * py.jobs.size(), cudaMemcpyHostToDevice));
-  ARD_CUDA(cudaMemcpy(dz, pz.jobs.data(), sizeof(XformJob) * pz.jobs.size(), cudaMemcpyHostToDevice));
-  const size_t rows_smem = (size_t)8 * ctx->maxn * sizeof(T), cols_smem = (size_t)33 * ctx->maxn * sizeof(T);
-  const int gb = ctx->num_sms * 8;
-  xform_rows_kernel<T><<<std::min(gb, (px.units + 7) / 8), 256, rows_smem, ctx->stream>>>(buf, dx, 1, px.units, ctx->maxn);
-  xform_cols_kernel<T><<<std::min(gb, py.units), 256, cols_smem, ctx->stream>>>(buf, dy, (int)py.jobs.size(), py.units);
-  xform_cols_kernel<T><<<std::min(gb, pz.units), 256, cols_smem, ctx->stream>>>(buf, dz, 1, pz.units);
+  ARD_CUDA(cudaMemcpy(dz, pz.jobs.data(), sizeof(XformJob), cudaMemcpyHostToDevice));
+  const int gb = ctx->num_sms * 4;
+  xform_gemm_kernel<T><<<std::min(gb, px.units), 256, 0, ctx->stream>>>(buf, dx, 1, px.units);
+  xform_gemm_kernel<T><<<std::min(gb, py.units), 256, 0, ctx->stream>>>(buf, dy, (int)py.jobs.size(), py.units);
+  xform_gemm_kernel<T><<<std::min(gb, pz.units), 256, 0, ctx->stream>>>(buf, dz, 1, pz.units);
   ARD_CUDA(cudaGetLastError());
-  // result is in scratch (b); move to out
   ARD_CUDA(cudaMemcpyAsync(buf + out, buf + b, sizeof(T) * (size_t)D.w * D.h * D.d, cudaMemcpyDeviceToDevice, ctx->stream));
   ARD_CUDA(cudaStreamSynchronize(ctx->stream));
   cudaFree(dx); cudaFree(dy); cudaFree(dz);
@@ -717,23 +740,24 @@ extern "C" int ard_set_initial_pressure(ard_ctx* c, int32_t scene, int32_t parti
   const DctDev& D = ctx->dct[idx];
   const long long N = (long long)D.w * D.h * D.d;
   const size_t es = elem_size(ctx);
-  // p0 -> M[1] (host upload), transform in place through the pool scratch, copy the level to M[0]
+  // p0 -> scratch (unpadded), transform there, then copy into both padded levels
   const long long s0 = ctx->scratch;
+  char* base = (char*)ctx->d_buf;
   if (ctx->prec == ARD_PREC_F64) {
     std::vector<double> h(pressure, pressure + N);
-    ARD_CUDA(cudaMemcpy((double*)ctx->d_buf + D.M[1], h.data(), N * es, cudaMemcpyHostToDevice));
+    ARD_CUDA(cudaMemcpy(base + (s0 + N) * es, h.data(), N * es, cudaMemcpyHostToDevice));
   } else {
-    ARD_CUDA(cudaMemcpy((float*)ctx->d_buf + D.M[1], pressure, N * es, cudaMemcpyHostToDevice));
+    ARD_CUDA(cudaMemcpy(base + (s0 + N) * es, pressure, N * es, cudaMemcpyHostToDevice));
   }
   // modes = DCT-II(p0) / (8 N s_i) with s_i = 1 / sqrt(2N)
   const double scale = 1.0 / (8.0 * (double)N / std::sqrt(2.0 * (double)N));
-  rc = ctx->prec == ARD_PREC_F64 ? ard::dense_transform<double>(ctx, D, D.M[1], D.M[1], s0, false, scale)
-                                 : ard::dense_transform<float>(ctx, D, D.M[1], D.M[1], s0, false, scale);
-  if (rc == ARD_OK) {
-    cudaError_t e = cudaMemcpy((char*)ctx->d_buf + D.M[0] * es, (char*)ctx->d_buf + D.M[1] * es, N * es, cudaMemcpyDeviceToDevice);
-    if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = ARD_ERR_CUDA; }
-  }
-  return rc;
+  rc = ctx->prec == ARD_PREC_F64 ? ard::dense_transform<double>(ctx, D, s0 + N, s0 + N, s0, false, scale)
+                                 : ard::dense_transform<float>(ctx, D, s0 + N, s0 + N, s0, false, scale);
+  if (rc) return rc;
+  for (int lvl = 0; lvl < 2; ++lvl)
+    ARD_CUDA(cudaMemcpy2D(base + D.M[lvl] * es, D.wp * es, base + (s0 + N) * es, D.w * es, D.w * es,
+                          (size_t)D.h * D.d, cudaMemcpyDeviceToDevice));
+  return ARD_OK;
 }
 
 extern "C" int ard_read_recorders_f64(ard_ctx* c, int32_t scene, double* out, int64_t t0, int64_t nt) {
@@ -780,8 +804,9 @@ extern "C" int ard_read_field(ard_ctx* c, int32_t scene, int32_t partition, floa
     const long long N = (long long)D.w * D.h * D.d;
     const long long s0 = ctx->scratch;
     char* base = (char*)ctx->d_buf;
-    // copy the modes to the scratch, transform there: p = s_i * Ci^T Ci^T Ci^T M
-    ARD_CUDA(cudaMemcpy(base + (s0 + 2 * N) * es, base + D.M[lvl] * es, N * es, cudaMemcpyDeviceToDevice));
+    // unpad the modes into the scratch, transform there: p = s_i * Ci^T Ci^T Ci^T M
+    ARD_CUDA(cudaMemcpy2D(base + (s0 + 2 * N) * es, D.w * es, base + D.M[lvl] * es, D.wp * es, D.w * es,
+                          (size_t)D.h * D.d, cudaMemcpyDeviceToDevice));
     rc = ctx->prec == ARD_PREC_F64 ? ard::dense_transform<double>(ctx, D, s0 + 2 * N, s0 + 2 * N, s0, true, D.si)
                                    : ard::dense_transform<float>(ctx, D, s0 + 2 * N, s0 + 2 * N, s0, true, D.si);
     if (rc == ARD_OK) {
