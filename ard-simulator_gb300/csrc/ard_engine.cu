@@ -84,6 +84,21 @@ static int validate_scene(const ard_scene& s, std::string* err) {
   return ARD_OK;
 }
 
+// Kernel attributes must be set on the instances this file launches (each
+// translation unit holds its own instances of the kernel templates): the FP64
+// modal kernel needs more than 48 KB of dynamic shared memory.
+static int configure_kernels(Ctx* ctx) {
+  const int modal_smem = (int)(kModalSmemElems * elem_size(ctx));
+  if (ctx->prec == ARD_PREC_F64) {
+    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
+    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
+  } else {
+    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
+    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
+  }
+  return ARD_OK;
+}
+
 extern "C" int ard_abi_version(void) { return ARD_ABI_VERSION; }
 
 extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_options* opt, ard_ctx** out) {
@@ -120,6 +135,7 @@ extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_o
   ctx->num_sms = prop.multiProcessorCount;
   ctx->smem_optin = (int)prop.sharedMemPerBlockOptin;
   int rc = build_layout(ctx.get(), scenes, n_scenes);
+  if (rc == ARD_OK) rc = configure_kernels(ctx.get());
   if (rc) {
     g_create_error = ctx->err;
     free_ctx_device(ctx.get());

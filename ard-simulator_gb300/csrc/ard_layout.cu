@@ -579,15 +579,6 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   ARD_CUDA(cudaStreamSynchronize(ctx->stream));
   if ((rc = upload_pml_zeta(ctx))) return rc;
   if ((rc = zero_state(ctx))) return rc;
-  // the FP64 modal kernel needs more than 48 KB of dynamic shared memory
-  const int modal_smem = (int)(kModalSmemElems * es);
-  if (ctx->prec == ARD_PREC_F64) {
-    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
-    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
-  } else {
-    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
-    ARD_CUDA(cudaFuncSetAttribute(modal_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
-  }
   ARD_CUDA(cudaStreamSynchronize(ctx->stream));
   return ARD_OK;
 }
