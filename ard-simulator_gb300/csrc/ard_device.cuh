@@ -58,7 +58,7 @@ struct DctDev {
   long long PX, PY, PZ;
   long long RX, RY, RZ;
   long long tmpX, tmpY, tmpZ;
-  long long cw, ch, cd;    // cosine tables of extents w, h, d: C then Ci (n*n each)
+  long long cw, ch, cd;    // cosine tables of extents w, h, d: C, Ci, C^T, Ci^T (n*n each)
   long long recpart;       // [ntiles][nrec]
   double sf;               // forward scale 1 / (2 sqrt(2N))
   double si;               // inverse scale 1 / sqrt(2N)
@@ -123,6 +123,22 @@ struct XformJob {
   int first;    // first 64 x 64 output tile of this job
   int tn;       // tiles along N
   int ntiles;
+  double scale;
+};
+
+// One fused 2D transform of a face layer, for output columns [u0, u0 + ub):
+//   T[r][c]   = sum_j X[r][j] B(j, u0 + c)        (along the fast axis U)
+//   Out[o][c] = scale sum_r A(o, r) T[r][c]        (along the slow axis V)
+// X (V x U, row pitch ld) = sum over nparts slabs of in0 + sgn * in1.
+// Forward: A = C_V, B(j, u) = C_U[u][j]; inverse: A(o, r) = Ci_V[r][o],
+// B(j, u) = Ci_U[j][u].  tabA / tabB point at row-contiguous copies.
+struct Face2DJob {
+  long long in0, in1, out;
+  long long part_stride;
+  long long tabA, tabB;
+  int nparts, sgn;
+  int V, U, ld;
+  int u0, ub;
   double scale;
 };
 

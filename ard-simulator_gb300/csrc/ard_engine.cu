@@ -89,12 +89,17 @@ static int validate_scene(const ard_scene& s, std::string* err) {
 // modal kernel needs more than 48 KB of dynamic shared memory.
 static int configure_kernels(Ctx* ctx) {
   const int modal_smem = (int)(kModalSmemElems * elem_size(ctx));
+  const int f2d = (int)std::max<size_t>(ctx->f2d_bytes, 1);
   if (ctx->prec == ARD_PREC_F64) {
     ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
     ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
+    if (ctx->fused_faces)
+      ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, f2d));
   } else {
     ARD_CUDA(cudaFuncSetAttribute(modal_kernel<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
     ARD_CUDA(cudaFuncSetAttribute(modal_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
+    if (ctx->fused_faces)
+      ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, f2d));
   }
   return ARD_OK;
 }
@@ -209,13 +214,20 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   if (!ctx->dct.empty()) {
     const int gx = ctx->num_sms * 4;
     ARD_CUDA(mark(kStageFwdRows));
-    xform_gemm_kernel<T><<<grid_for(ctx->fwd1.units, 1, gx), 256, 0, s>>>(buf, ctx->d_fwd1, (int)ctx->fwd1.jobs.size(),
-                                                                           ctx->fwd1.units);
+    if (ctx->fused_faces) {
+      face2d_kernel<T><<<grid_for((long long)ctx->fwd2d.size(), 1, gx), 256, ctx->f2d_bytes, s>>>(
+          buf, ctx->d_fwd2d, (int)ctx->fwd2d.size(), ctx->f2d_smem);
+    } else {
+      xform_gemm_kernel<T><<<grid_for(ctx->fwd1.units, 1, gx), 256, 0, s>>>(buf, ctx->d_fwd1, (int)ctx->fwd1.jobs.size(),
+                                                                             ctx->fwd1.units);
+    }
     ARD_CUDA(cudaGetLastError());
     ARD_CUDA(mark(kStageFwdCols));
-    xform_gemm_kernel<T><<<grid_for(ctx->fwd2.units, 1, gx), 256, 0, s>>>(buf, ctx->d_fwd2, (int)ctx->fwd2.jobs.size(),
-                                                                           ctx->fwd2.units);
-    ARD_CUDA(cudaGetLastError());
+    if (!ctx->fused_faces) {
+      xform_gemm_kernel<T><<<grid_for(ctx->fwd2.units, 1, gx), 256, 0, s>>>(buf, ctx->d_fwd2, (int)ctx->fwd2.jobs.size(),
+                                                                             ctx->fwd2.units);
+      ARD_CUDA(cudaGetLastError());
+    }
     ModalArgs<T> ma{buf, ctx->d_dct, ctx->d_tiles, (int)ctx->tiles.size(), ctx->d_srcpts, ctx->d_recpts,
                     ctx->d_series, ctx->max_steps, ctx->d_t, tstep, par};
     ARD_CUDA(mark(kStageModal));
@@ -233,13 +245,20 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
       ARD_CUDA(cudaGetLastError());
     }
     ARD_CUDA(mark(kStageInvCols));
-    xform_gemm_kernel<T><<<grid_for(ctx->inv1.units, 1, gx), 256, 0, s>>>(buf, ctx->d_inv1, (int)ctx->inv1.jobs.size(),
-                                                                           ctx->inv1.units);
+    if (ctx->fused_faces) {
+      face2d_kernel<T><<<grid_for((long long)ctx->inv2d.size(), 1, gx), 256, ctx->f2d_bytes, s>>>(
+          buf, ctx->d_inv2d, (int)ctx->inv2d.size(), ctx->f2d_smem);
+    } else {
+      xform_gemm_kernel<T><<<grid_for(ctx->inv1.units, 1, gx), 256, 0, s>>>(buf, ctx->d_inv1, (int)ctx->inv1.jobs.size(),
+                                                                             ctx->inv1.units);
+    }
     ARD_CUDA(cudaGetLastError());
     ARD_CUDA(mark(kStageInvRows));
-    xform_gemm_kernel<T><<<grid_for(ctx->inv2.units, 1, gx), 256, 0, s>>>(buf, ctx->d_inv2, (int)ctx->inv2.jobs.size(),
-                                                                           ctx->inv2.units);
-    ARD_CUDA(cudaGetLastError());
+    if (!ctx->fused_faces) {
+      xform_gemm_kernel<T><<<grid_for(ctx->inv2.units, 1, gx), 256, 0, s>>>(buf, ctx->d_inv2, (int)ctx->inv2.jobs.size(),
+                                                                             ctx->inv2.units);
+      ARD_CUDA(cudaGetLastError());
+    }
   }
   if (fork) {
     ARD_CUDA(cudaEventRecord(ctx->ev_join, s2));

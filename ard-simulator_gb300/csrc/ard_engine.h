@@ -10,6 +10,7 @@
 
 #include "ard_device.cuh"
 #include "ard_gb300.h"
+#include "ard_kernels.cuh"
 
 namespace ard {
 
@@ -54,7 +55,11 @@ struct Ctx {
   std::vector<unsigned char> masks;
   std::vector<PointDev> srcpts, recpts;
   std::vector<int4> tiles;
-  JobList fwd1, fwd2, inv1, inv2;
+  JobList fwd1, fwd2, inv1, inv2;           // two-pass GEMM face transforms
+  std::vector<Face2DJob> fwd2d, inv2d;      // fused face transforms
+  bool fused_faces = false;
+  Face2DSmem f2d_smem{0, 0, 0};
+  size_t f2d_bytes = 0;
   std::vector<std::pair<int, long long>> cos_tables;  // extent -> offset
   long long n_pml_cells = 0, n_face_cells = 0;
   long long n_air_cells = 0;
@@ -74,6 +79,7 @@ struct Ctx {
   PointDev* d_recpts = nullptr;
   int4* d_tiles = nullptr;
   XformJob *d_fwd1 = nullptr, *d_fwd2 = nullptr, *d_inv1 = nullptr, *d_inv2 = nullptr;
+  Face2DJob *d_fwd2d = nullptr, *d_inv2d = nullptr;
   float* d_series = nullptr;
   double* d_hist = nullptr;
   long long* d_t = nullptr;

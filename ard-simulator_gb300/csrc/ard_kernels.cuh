@@ -58,6 +58,32 @@ __device__ __forceinline__ void store4(double* p, const double (&r)[4]) {
   reinterpret_cast<double2*>(p)[1] = make_double2(r[2], r[3]);
 }
 
+// ---- asynchronous global -> shared copies (cp.async, L2-cached) ----
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  const int n = valid ? 16 : 0;  // 0: zero-fill, nothing is read
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_scalar(float* smem, const float* gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  const int n = valid ? 4 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_scalar(double* smem, const double* gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  const int n = valid ? 8 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
+}
+// 4 consecutive elements (16 B for float, 2 x 16 B for double)
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem, bool valid) { cp_async16(smem, gmem, valid); }
+__device__ __forceinline__ void cp_async4(double* smem, const double* gmem, bool valid) {
+  cp_async16(smem, gmem, valid);
+  cp_async16(smem + 2, gmem + 2, valid);
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -167,6 +193,106 @@ __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, co
 }
 
 // ---------------------------------------------------------------------------
+// Fused face transform: one block per (face layer, 32-column slab); the
+// layer is staged in shared memory, the U-transform of the slab goes to
+// shared memory, the V-transform writes the output slab.
+// ---------------------------------------------------------------------------
+
+struct Face2DSmem {
+  int xs;  // elements for X (and later A): max(V * xp, V * ap)
+  int bs;  // U * 33
+  int ts;  // V * 33
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) face2d_kernel(T* __restrict__ buf, const Face2DJob* __restrict__ jobs,
+                                                      int njobs, Face2DSmem sm) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* Xs = reinterpret_cast<T*>(smem_raw);
+  T* Bs = Xs + sm.xs;
+  T* Ts = Bs + sm.bs;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int jb = blockIdx.x; jb < njobs; jb += gridDim.x) {
+    const Face2DJob J = jobs[jb];
+    const int V = J.V, U = J.U;
+    const int xp = ((U + 3) & ~3) + 4;
+    const int ap = ((V + 3) & ~3) + 4;
+    __syncthreads();  // previous job done with shared memory
+    for (int i = tid; i < V * xp; i += 256) {
+      const int r = i / xp, j = i - r * xp;
+      T v = 0;
+      if (j < U) {
+        const long long off = (long long)r * J.ld + j;
+        for (int b = 0; b < J.nparts; ++b) {
+          const long long o = (long long)b * J.part_stride + off;
+          v += buf[J.in0 + o];
+          if (J.in1 >= 0) v += (T)J.sgn * buf[J.in1 + o];
+        }
+      }
+      Xs[i] = v;
+    }
+    const T* B = buf + J.tabB;
+    for (int i = tid; i < ((U + 3) & ~3) * 32; i += 256) {
+      const int j = i >> 5, c = i & 31;
+      Bs[j * 33 + c] = (j < U && c < J.ub) ? B[(long long)j * U + J.u0 + c] : (T)0;
+    }
+    __syncthreads();
+    // T = X B (slab): lane = column, warp = row group
+    for (int r0 = warp; r0 < V; r0 += 32) {
+      T acc[4] = {0, 0, 0, 0};
+      int rr[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) rr[i] = min(r0 + 8 * i, V - 1);
+      for (int j = 0; j < U; j += 4) {
+        const T b0 = Bs[j * 33 + lane], b1 = Bs[(j + 1) * 33 + lane];
+        const T b2 = Bs[(j + 2) * 33 + lane], b3 = Bs[(j + 3) * 33 + lane];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          T x[4];
+          load4(Xs + rr[i] * xp + j, x);
+          acc[i] += x[0] * b0 + x[1] * b1 + x[2] * b2 + x[3] * b3;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (r0 + 8 * i < V) Ts[(r0 + 8 * i) * 33 + lane] = acc[i];
+    }
+    __syncthreads();
+    // A (V x V, row o contiguous) into the X area
+    const T* A = buf + J.tabA;
+    for (int i = tid; i < V * ap; i += 256) {
+      const int o = i / ap, r = i - o * ap;
+      Xs[i] = r < V ? A[(long long)o * V + r] : (T)0;
+    }
+    __syncthreads();
+    const T scale = (T)J.scale;
+    for (int o0 = warp; o0 < V; o0 += 32) {
+      T acc[4] = {0, 0, 0, 0};
+      int oo[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) oo[i] = min(o0 + 8 * i, V - 1);
+      for (int r = 0; r < V; r += 4) {
+        const T t0 = Ts[r * 33 + lane];
+        const T t1 = (r + 1 < V) ? Ts[(r + 1) * 33 + lane] : (T)0;
+        const T t2 = (r + 2 < V) ? Ts[(r + 2) * 33 + lane] : (T)0;
+        const T t3 = (r + 3 < V) ? Ts[(r + 3) * 33 + lane] : (T)0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          T a4[4];
+          load4(Xs + oo[i] * ap + r, a4);
+          acc[i] += a4[0] * t0 + a4[1] * t1 + a4[2] * t2 + a4[3] * t3;
+        }
+      }
+      if (lane < J.ub) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (o0 + 8 * i < V) buf[J.out + (long long)(o0 + 8 * i) * J.ld + J.u0 + lane] = acc[i] * scale;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Modal update
 // ---------------------------------------------------------------------------
 
@@ -185,9 +311,13 @@ struct ModalArgs {
   int par;
 };
 
-// Shared memory of the modal kernel, in elements of T.
+// Shared memory of the modal kernel, in elements of T: the ky-contraction
+// slots, point coefficients, recorder reduction, and the double-buffered
+// per-plane inputs (7 four-element rows per thread + 6 PX values per ky row).
 constexpr int kModalRySlot = 3 * 1024;  // [3 n][rpc * kxt = 1024]
-constexpr int kModalSmemElems = 2 * kModalRySlot + 2 * kMaxPointsPerPart * 128 + 8 * kMaxPointsPerPart;
+constexpr int kModalStage = 7 * 4 * kModalThreads + 32 * 6;
+constexpr int kModalSmemElems =
+    2 * kModalRySlot + 2 * kMaxPointsPerPart * 128 + 8 * kMaxPointsPerPart + 2 * kModalStage;
 
 // One block (8 warps) per tile of kxt kx x rpc ky x TZ kz modes; a thread
 // owns 4 consecutive kx of one ky row.  Per mode it reads M(t-1), M(t-2)
@@ -203,6 +333,7 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
   T* cws = ry_s + 2 * kModalRySlot;                  // [kMaxPointsPerPart][128]
   T* cwr = cws + kMaxPointsPerPart * 128;            // [kMaxPointsPerPart][128]
   T* red = cwr + kMaxPointsPerPart * 128;            // [8 warps][kMaxPointsPerPart]
+  T* stage = red + 8 * kMaxPointsPerPart;            // [2][kModalStage]
   __shared__ int pts_y[2][kMaxPointsPerPart], pts_z[2][kMaxPointsPerPart];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   T* __restrict__ buf = a.buf;
@@ -287,8 +418,28 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
     const T* tabB = buf + D.tabB;
     const T damping = (T)D.damping;
 
-    auto body = [&](auto parity, int kz) {
+    // per-plane inputs of plane kz into stage buffer sb (asynchronous)
+    auto issue = [&](int kz, int sb) {
+      T* st = stage + sb * kModalStage;
+      const long long row = ((long long)kz * h + (rowok ? ky : 0)) * wp + (lanok ? kx0 : 0);
+      cp_async4(st + (0 * kModalThreads + tid) * 4, Mcur + row, lanok);
+      cp_async4(st + (1 * kModalThreads + tid) * 4, Mout + row, lanok);
+      cp_async4(st + (2 * kModalThreads + tid) * 4, tabA + row, lanok);
+      cp_async4(st + (3 * kModalThreads + tid) * 4, tabB + row, lanok);
+#pragma unroll
+      for (int n = 0; n < 3; ++n)
+        cp_async4(st + ((4 + n) * kModalThreads + tid) * 4,
+                  PYr + n * planeY + (long long)kz * wp + (lanok ? kx0 : 0), lanok);
+      if (li < 6) {
+        const int pm = li / 3, n = li - pm * 3;
+        cp_async_scalar(st + 7 * 4 * kModalThreads + rs * 6 + li,
+                        PX + (pm * 3 + n) * planeX + (long long)kz * h + (rowok ? ky : 0), rowok);
+      }
+    };
+
+    auto body = [&](auto parity, int kz, int sb) {
       constexpr int PZ = decltype(parity)::value;  // kz & 1 (kz0 is even)
+      const T* st = stage + sb * kModalStage;
       T cz[3];
 #pragma unroll
       for (int n = 0; n < 3; ++n) cz[n] = Cd[(long long)kz * d + n];
@@ -297,24 +448,19 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
 #pragma unroll
       for (int pm = 0; pm < 2; ++pm)
 #pragma unroll
-        for (int n = 0; n < 3; ++n) px[pm][n] = rowok ? PX[(pm * 3 + n) * planeX + (long long)kz * h + ky] : (T)0;
+        for (int n = 0; n < 3; ++n) px[pm][n] = st[7 * 4 * kModalThreads + rs * 6 + pm * 3 + n];
       T py[3][4];
       T m[4], mp[4], ta[4], tb[4];
       const long long row = ((long long)kz * h + ky) * wp + kx0;
-      if (lanok) {
+      load4(st + (0 * kModalThreads + tid) * 4, m);
+      load4(st + (1 * kModalThreads + tid) * 4, mp);
+      load4(st + (2 * kModalThreads + tid) * 4, ta);
+      load4(st + (3 * kModalThreads + tid) * 4, tb);
 #pragma unroll
-        for (int n = 0; n < 3; ++n) load4(PYr + n * planeY + (long long)kz * wp + kx0, py[n]);
-        load4(Mcur + row, m);
-        load4(Mout + row, mp);
-        load4(tabA + row, ta);
-        load4(tabB + row, tb);
-      } else {
+      for (int n = 0; n < 3; ++n) load4(st + ((4 + n) * kModalThreads + tid) * 4, py[n]);
+      if (!lanok) {
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          py[0][e] = py[1][e] = py[2][e] = 0;
-          m[e] = mp[e] = ta[e] = 0;
-          tb[e] = 1;
-        }
+        for (int e = 0; e < 4; ++e) tb[e] = 1;  // keeps the reference arithmetic finite on idle lanes
       }
       T F[4];
 #pragma unroll
@@ -395,10 +541,24 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
       }
     };
 
+    // software pipeline: plane kz+1 loads while plane kz computes
+    issue(kz0, 0);
+    cp_async_commit();
     for (int kz = kz0; kz < kz1; kz += 2) {
-      body(std::integral_constant<int, 0>{}, kz);
-      if (kz + 1 < kz1) body(std::integral_constant<int, 1>{}, kz + 1);
+      if (kz + 1 < kz1) issue(kz + 1, 1);
+      cp_async_commit();
+      cp_async_wait<1>();
+      __syncwarp();
+      body(std::integral_constant<int, 0>{}, kz, 0);
+      if (kz + 1 < kz1) {
+        if (kz + 2 < kz1) issue(kz + 2, 0);
+        cp_async_commit();
+        cp_async_wait<1>();
+        __syncwarp();
+        body(std::integral_constant<int, 1>{}, kz + 1, 1);
+      }
     }
+    cp_async_wait<0>();
     if (lanok) {
 #pragma unroll
       for (int pm = 0; pm < 2; ++pm)
@@ -461,21 +621,28 @@ struct PmlArgs {
 // Grote-Sim PML (pml_partition.cpp:113-200) in slab coordinates: layer l
 // along the normal, (a, b) in the plane; outside the slab every field reads
 // zero (the reference's sentinel cell).  Only the normal damping zeta_n is
-// non-zero in a slab (zeta_a = zeta_b = 0 in the reference's formulas).  A
-// thread owns one (a, b) column and keeps p and phi_n of all layers in
-// registers; in-plane neighbours come through L1.
+// non-zero in a slab (zeta_a = zeta_b = 0 in the reference's formulas).
+// A block owns an 8 x 32 plane tile and walks the layers: the tile of p (halo
+// 3) and of phi_a / phi_b (halo 2 along their own axis) is staged in shared
+// memory per layer; the normal-axis stencils run from a register window.
 template <typename T>
-__global__ void __launch_bounds__(256, 2) pml_kernel(PmlArgs<T> a) {
+__global__ void __launch_bounds__(256) pml_kernel(PmlArgs<T> a) {
+  constexpr int TA = 8, TB = 32;
+  __shared__ T Ps[TA + 6][TB + 6];
+  __shared__ T FA[TA + 4][TB];
+  __shared__ T FB[TA][TB + 4];
   const T c7[7] = {2, -27, 270, -490, 270, -27, 2};
   const T c5[5] = {1, -8, 0, 8, -1};
+  const int tb = threadIdx.x & 31, ta = threadIdx.x >> 5;
   for (int bi = blockIdx.x; bi < a.nblocks; bi += gridDim.x) {
     const int4 blk = a.blocks[bi];
     const PmlDev& P = a.pml[blk.x];
-    const int ia = blk.y + (threadIdx.x >> 5), ib = blk.z + (threadIdx.x & 31);
-    if (ia >= P.A || ib >= P.B) continue;
     const int L = P.L, A = P.A, B = P.B;
+    const int a0 = blk.y, b0 = blk.z;
+    const int ia = a0 + ta, ib = b0 + tb;
+    const bool inside = ia < A && ib < B;
     const long long lstride = (long long)A * B;
-    const long long col = (long long)ia * B + ib;
+    const long long col = inside ? (long long)ia * B + ib : 0;
     const T* p = a.buf + P.p[a.par ^ 1];   // p(t-1)
     T* pn = a.buf + P.p[a.par];            // p(t-2) -> p(t)
     const T* fn = a.buf + P.phn[a.par ^ 1];
@@ -486,57 +653,81 @@ __global__ void __launch_bounds__(256, 2) pml_kernel(PmlArgs<T> a) {
     T* fb_o = a.buf + P.phb[a.par];
     const T* zeta = a.buf + P.zeta;
     const T* force = a.buf + P.force;
-    T pc[kMaxPmlLayers + 6], fc[kMaxPmlLayers + 4];
+    // register windows along the normal: p(l-3 .. l+3), phi_n(l-2 .. l+2)
+    T pw[7], fw[5];
 #pragma unroll
-    for (int l = 0; l < kMaxPmlLayers + 6; ++l) {
-      const int ll = l - 3;
-      pc[l] = (ll >= 0 && ll < L) ? p[ll * lstride + col] : (T)0;
+    for (int m = 0; m < 7; ++m) {
+      const int ll = m - 3;
+      pw[m] = (inside && ll >= 0 && ll < L) ? p[ll * lstride + col] : (T)0;
     }
 #pragma unroll
-    for (int l = 0; l < kMaxPmlLayers + 4; ++l) {
-      const int ll = l - 2;
-      fc[l] = (ll >= 0 && ll < L) ? fn[ll * lstride + col] : (T)0;
+    for (int m = 0; m < 5; ++m) {
+      const int ll = m - 2;
+      fw[m] = (inside && ll >= 0 && ll < L) ? fn[ll * lstride + col] : (T)0;
     }
     const T d180 = (T)180 * a.dh * a.dh, d12 = (T)12 * a.dh;
-#pragma unroll
-    for (int l = 0; l < kMaxPmlLayers; ++l) {
-      if (l >= L) break;
-      const long long I = l * lstride + col;
+    for (int l = 0; l < L; ++l) {
       const T* pl = p + l * lstride;
-      T ln = 0, la = 0, lb = 0, un = 0, ua = 0, ub = 0, gn = 0, ga = 0, gb = 0;
-#pragma unroll
-      for (int m = 0; m < 7; ++m) {
-        const int aa = ia + m - 3, bb = ib + m - 3;
-        ln += c7[m] * pc[l + m];
-        la += c7[m] * ((aa >= 0 && aa < A) ? pl[(long long)aa * B + ib] : (T)0);
-        lb += c7[m] * ((bb >= 0 && bb < B) ? pl[(long long)ia * B + bb] : (T)0);
+      const T* fal = fa + l * lstride;
+      const T* fbl = fb + l * lstride;
+      __syncthreads();  // previous layer done with the tiles
+      for (int i = threadIdx.x; i < (TA + 6) * (TB + 6); i += 256) {
+        const int r = i / (TB + 6), c = i - r * (TB + 6);
+        const int aa = a0 + r - 3, bb = b0 + c - 3;
+        Ps[r][c] = (aa >= 0 && aa < A && bb >= 0 && bb < B) ? pl[(long long)aa * B + bb] : (T)0;
       }
-#pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        const int aa = ia + m - 2, bb = ib + m - 2;
-        const T pa = (aa >= 0 && aa < A) ? pl[(long long)aa * B + ib] : (T)0;
-        const T pb = (bb >= 0 && bb < B) ? pl[(long long)ia * B + bb] : (T)0;
-        un += c5[m] * pc[l + m + 1];
-        ua += c5[m] * pa;
-        ub += c5[m] * pb;
-        gn += c5[m] * fc[l + m];
-        ga += c5[m] * ((aa >= 0 && aa < A) ? fa[l * lstride + (long long)aa * B + ib] : (T)0);
-        gb += c5[m] * ((bb >= 0 && bb < B) ? fb[l * lstride + (long long)ia * B + bb] : (T)0);
+      for (int i = threadIdx.x; i < (TA + 4) * TB; i += 256) {
+        const int r = i / TB, c = i - r * TB;
+        const int aa = a0 + r - 2, bb = b0 + c;
+        FA[r][c] = (aa >= 0 && aa < A && bb < B) ? fal[(long long)aa * B + bb] : (T)0;
       }
-      ln /= d180; la /= d180; lb /= d180;
-      un /= d12; ua /= d12; ub /= d12;
-      gn /= d12; ga /= d12; gb /= d12;
-      const T zn = zeta[l];
-      const T pcur = pc[l + 3], pold = pn[I];
-      const int sl = l - P.strip0;
-      const T f = (sl >= 0 && sl < 3) ? force[sl * lstride + col] : (T)0;
-      const T t3 = a.c0 * a.c0 * (ln + la + lb);
-      const T t4 = -zn * (pcur - pold) / a.dt;
-      pn[I] = (T)2 * pcur - pold + a.dt * a.dt * (t3 + t4 + (gn + ga + gb) + f);
-      const T fnc = fc[l + 2];
-      fn_o[I] = fnc - a.dt * zn * fnc + a.dt * (-zn) * un;
-      fa_o[I] = fa[I] + a.dt * zn * ua;
-      fb_o[I] = fb[I] + a.dt * zn * ub;
+      for (int i = threadIdx.x; i < TA * (TB + 4); i += 256) {
+        const int r = i / (TB + 4), c = i - r * (TB + 4);
+        const int aa = a0 + r, bb = b0 + c - 2;
+        FB[r][c] = (aa < A && bb >= 0 && bb < B) ? fbl[(long long)aa * B + bb] : (T)0;
+      }
+      __syncthreads();
+      if (inside) {
+        T ln = 0, la = 0, lb = 0;
+#pragma unroll
+        for (int m = 0; m < 7; ++m) {
+          ln += c7[m] * pw[m];
+          la += c7[m] * Ps[ta + m][tb + 3];
+          lb += c7[m] * Ps[ta + 3][tb + m];
+        }
+        T un = 0, ua = 0, ub = 0, gn = 0, ga = 0, gb = 0;
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+          un += c5[m] * pw[m + 1];
+          ua += c5[m] * Ps[ta + 1 + m][tb + 3];
+          ub += c5[m] * Ps[ta + 3][tb + 1 + m];
+          gn += c5[m] * fw[m];
+          ga += c5[m] * FA[ta + m][tb];
+          gb += c5[m] * FB[ta][tb + m];
+        }
+        ln /= d180; la /= d180; lb /= d180;
+        un /= d12; ua /= d12; ub /= d12;
+        gn /= d12; ga /= d12; gb /= d12;
+        const long long I = l * lstride + col;
+        const T zn = zeta[l];
+        const T pcur = pw[3], pold = pn[I];
+        const int sl = l - P.strip0;
+        const T f = (sl >= 0 && sl < 3) ? force[sl * lstride + col] : (T)0;
+        const T t3 = a.c0 * a.c0 * (ln + la + lb);
+        const T t4 = -zn * (pcur - pold) / a.dt;
+        pn[I] = (T)2 * pcur - pold + a.dt * a.dt * (t3 + t4 + (gn + ga + gb) + f);
+        const T fnc = fw[2];
+        fn_o[I] = fnc - a.dt * zn * fnc + a.dt * (-zn) * un;
+        fa_o[I] = FA[ta + 2][tb] + a.dt * zn * ua;
+        fb_o[I] = FB[ta][tb + 2] + a.dt * zn * ub;
+      }
+      // slide the windows one layer
+#pragma unroll
+      for (int m = 0; m < 6; ++m) pw[m] = pw[m + 1];
+      pw[6] = (inside && l + 4 < L) ? p[(l + 4) * lstride + col] : (T)0;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) fw[m] = fw[m + 1];
+      fw[4] = (inside && l + 3 < L) ? fn[(l + 3) * lstride + col] : (T)0;
     }
   }
 }
@@ -645,9 +836,10 @@ static __global__ void advance_time_kernel(long long* tcount, int n) {
 
 // ---- setup kernels (FP64 arithmetic) ----
 
-// Per extent n, two n*n tables: C[k][j] = 2 cos(pi (j + 1/2) k / n) (the
-// REDFT10 matrix) and the REDFT01 matrix Ci[k][j] = C[k][j] with row k = 0
-// halved (REDFT01 weights X_0 by 1, the others by 2).
+// Per extent n, four n*n tables: C[k][j] = 2 cos(pi (j + 1/2) k / n) (the
+// REDFT10 matrix), the REDFT01 matrix Ci[k][j] = C[k][j] with row k = 0
+// halved (REDFT01 weights X_0 by 1, the others by 2), and the transposes of
+// both (row-contiguous access for the fused face transforms).
 template <typename T>
 __global__ void cos_table_kernel(T* buf, long long off, int n) {
   const long long nn = (long long)n * n;
@@ -655,8 +847,12 @@ __global__ void cos_table_kernel(T* buf, long long off, int n) {
     const int k = (int)(i / n), j = (int)(i - (long long)k * n);
     const long long q = ((long long)(2 * j + 1) * k) % (4LL * n);  // argument reduced exactly in integers
     const double v = 2.0 * cospi((double)q / (2.0 * n));
+    const double vi = k == 0 ? 0.5 * v : v;
+    const long long t = (long long)j * n + k;
     buf[off + i] = (T)v;
-    buf[off + nn + i] = (T)(k == 0 ? 0.5 * v : v);
+    buf[off + nn + i] = (T)vi;
+    buf[off + 2 * nn + t] = (T)v;
+    buf[off + 3 * nn + t] = (T)vi;
   }
 }
 

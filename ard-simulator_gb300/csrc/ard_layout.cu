@@ -165,7 +165,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   auto cos_table = [&](int n) {
     auto it = cos_off.find(n);
     if (it != cos_off.end()) return it->second;
-    const long long o = pool.take(2LL * n * n);
+    const long long o = pool.take(4LL * n * n);
     cos_off[n] = o;
     ctx->maxn = std::max(ctx->maxn, n);
     return o;
@@ -283,10 +283,11 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     D.nby = (D.h + D.rpc - 1) / D.rpc;
     col_tiles += (long long)D.nbx * D.nby;
   }
-  const long long target = (long long)ctx->num_sms * 2;
+  // resident slots: 2 tiles per SM; split kz only while the tiles still fit one wave
+  const long long slots = (long long)ctx->num_sms * 2;
   for (size_t k = 0; k < ctx->dct.size(); ++k) {
     DctDev& D = ctx->dct[k];
-    long long nbz = col_tiles > 0 ? (target + col_tiles - 1) / col_tiles : 1;
+    long long nbz = col_tiles > 0 ? slots / col_tiles : 1;
     nbz = std::max(1LL, std::min<long long>(nbz, D.d / 2));
     int TZ = (int)((D.d + nbz - 1) / nbz);
     if (TZ < D.d) TZ += TZ & 1;  // even, so every kz tile starts on an even plane
@@ -512,6 +513,51 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     }
   }
 
+  // ---- fused face transforms (one kernel per direction) when a layer fits in shared memory ----
+  {
+    const size_t es0 = elem_size(ctx);
+    long long xs = 0, bs = 0, ts = 0;
+    for (const DctDev& D : ctx->dct) {
+      struct Ax { long long f, p, P, R; int U, V, ld; long long cU, cV; int nb; };
+      const Ax axes[3] = {{D.fX, D.pX, D.PX, D.RX, D.h, D.d, D.h, D.ch, D.cd, D.nbx},
+                          {D.fY, D.pY, D.PY, D.RY, D.w, D.d, D.wp, D.cw, D.cd, D.nby},
+                          {D.fZ, D.pZ, D.PZ, D.RZ, D.w, D.h, D.wp, D.cw, D.ch, D.nbz}};
+      for (const Ax& a : axes) {
+        const long long LS = (long long)a.V * a.ld;
+        const long long UU = (long long)a.U * a.U, VV = (long long)a.V * a.V;
+        xs = std::max(xs, std::max((long long)a.V * (((a.U + 3) & ~3) + 4), (long long)a.V * (((a.V + 3) & ~3) + 4)));
+        bs = std::max(bs, (long long)((a.U + 3) & ~3) * 33);
+        ts = std::max(ts, (long long)a.V * 33);
+        for (int u0 = 0; u0 < a.U; u0 += 32) {
+          const int ub = std::min(32, a.U - u0);
+          for (int pm = 0; pm < 2; ++pm)
+            for (int n = 0; n < 3; ++n) {
+              Face2DJob j{};
+              j.in0 = a.f + n * LS; j.in1 = a.f + (5 - n) * LS; j.sgn = pm ? -1 : 1;
+              j.nparts = 1; j.part_stride = 0;
+              j.out = a.P + (pm * 3 + n) * LS;
+              j.tabA = a.cV; j.tabB = a.cU + 2 * UU;
+              j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.sf;
+              ctx->fwd2d.push_back(j);
+            }
+          for (int L = 0; L < 6; ++L) {
+            const int n = L < 3 ? L : 5 - L;
+            Face2DJob j{};
+            j.in0 = a.R + n * LS; j.in1 = a.R + (3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
+            j.nparts = a.nb; j.part_stride = 6 * LS;
+            j.out = a.p + L * LS;
+            j.tabA = a.cV + 3 * VV; j.tabB = a.cU + UU;
+            j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.si;
+            ctx->inv2d.push_back(j);
+          }
+        }
+      }
+    }
+    ctx->f2d_smem = Face2DSmem{(int)xs, (int)bs, (int)ts};
+    ctx->f2d_bytes = (size_t)(xs + bs + ts) * es0;
+    ctx->fused_faces = !ctx->dct.empty() && ctx->f2d_bytes <= (size_t)std::min(ctx->smem_optin, 200 * 1024);
+  }
+
   // ---- device allocation ----
   const size_t es = elem_size(ctx);
   ctx->pool_elems = pool.off;
@@ -542,6 +588,8 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   if ((rc = up(&ctx->d_fwd2, ctx->fwd2.jobs))) return rc;
   if ((rc = up(&ctx->d_inv1, ctx->inv1.jobs))) return rc;
   if ((rc = up(&ctx->d_inv2, ctx->inv2.jobs))) return rc;
+  if ((rc = up(&ctx->d_fwd2d, ctx->fwd2d))) return rc;
+  if ((rc = up(&ctx->d_inv2d, ctx->inv2d))) return rc;
   ARD_CUDA(cudaMalloc(&ctx->d_series, sizeof(float) * std::max(1LL, (long long)ctx->n_src_total * ctx->max_steps)));
   ARD_CUDA(cudaMemset(ctx->d_series, 0, sizeof(float) * (long long)ctx->n_src_total * ctx->max_steps));
   ARD_CUDA(cudaMalloc(&ctx->d_hist, sizeof(double) * std::max(1LL, (long long)ctx->n_rec_total * ctx->max_steps)));
@@ -586,7 +634,8 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
 void free_ctx_device(Ctx* ctx) {
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   void* ptrs[] = {ctx->d_buf, ctx->d_mask, ctx->d_dct, ctx->d_pml, ctx->d_pml_blocks, ctx->d_ifs, ctx->d_srcpts,
-                  ctx->d_recpts, ctx->d_tiles, ctx->d_fwd1, ctx->d_fwd2, ctx->d_inv1, ctx->d_inv2, ctx->d_series,
+                  ctx->d_recpts, ctx->d_tiles, ctx->d_fwd1, ctx->d_fwd2, ctx->d_inv1, ctx->d_inv2, ctx->d_fwd2d,
+                  ctx->d_inv2d, ctx->d_series,
                   ctx->d_hist, ctx->d_t};
   for (void* p : ptrs)
     if (p) cudaFree(p);
