@@ -7,6 +7,7 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -120,6 +121,11 @@ extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_o
   ctx->use_graphs = opt ? (opt->use_graphs != 0) : true;
   ctx->device = opt ? opt->device : 0;
   ctx->arith = opt ? opt->arithmetic : ARD_ARITH_ACCURATE;
+  {
+    const char* dbg = std::getenv("ARD_DEBUG_SYNC");
+    ctx->debug_sync = dbg && dbg[0] == '1';
+    if (ctx->debug_sync) ctx->use_graphs = false;
+  }
   if (ctx->arith != ARD_ARITH_ACCURATE && ctx->arith != ARD_ARITH_REFERENCE) {
     g_create_error = "ard_create: bad arithmetic mode";
     return ARD_ERR_INVALID;
@@ -197,7 +203,20 @@ namespace ard {
 template <typename T>
 int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, bool fork, cudaEvent_t* ev) {
   T* buf = reinterpret_cast<T*>(ctx->d_buf);
-  auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], s) : cudaSuccess; };
+  // checked mode (ARD_DEBUG_SYNC=1): every stage is synchronised and its error
+  // reported with the stage name, so a failing kernel is identified
+  const char* stage_names[] = {"pml", "fwd", "fwd2", "modal", "recorder", "inv", "inv2", "iface", "end"};
+  auto mark = [&](int k) -> cudaError_t {
+    if (ctx->debug_sync && k > 0) {
+      cudaError_t e = cudaStreamSynchronize(s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s2);
+      if (e != cudaSuccess) {
+        std::fprintf(stderr, "ard: stage before '%s' failed: %s\n", stage_names[k], cudaGetErrorString(e));
+        return e;
+      }
+    }
+    return ev ? cudaEventRecord(ev[k], s) : cudaSuccess;
+  };
   // PML branch depends only on the previous step's interface forcing
   if (fork) {
     ARD_CUDA(cudaEventRecord(ctx->ev_fork, s));
@@ -344,6 +363,10 @@ extern "C" int ard_step(ard_ctx* c, int64_t nsteps, void* stream) {
   if (s != ctx->stream) {
     ARD_CUDA(cudaEventRecord(ctx->ev_join, s));
     ARD_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+  }
+  if (ctx->debug_sync) {
+    ARD_CUDA(cudaStreamSynchronize(s));
+    return check_guards(ctx);
   }
   return ARD_OK;
 }

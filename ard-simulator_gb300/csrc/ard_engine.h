@@ -41,6 +41,7 @@ struct Ctx {
   int smem_optin = 48 * 1024;
   long long max_steps = 4096;
   bool use_graphs = true;
+  bool debug_sync = false;          // ARD_DEBUG_SYNC=1: synchronise and check after every stage
   int graph_steps = 32;
   double dh = 0, dt = 0, c0 = 0, pml_R = 1e-5, damping = 0.999;
   int pml_layers = 0;
@@ -70,6 +71,8 @@ struct Ctx {
 
   // device memory
   void* d_buf = nullptr;          // element pool (float or double)
+  void* d_buf_base = nullptr;     // allocation holding the pool (and guards in checked mode)
+  size_t guard_bytes = 0;
   unsigned char* d_mask = nullptr;
   DctDev* d_dct = nullptr;
   PmlDev* d_pml = nullptr;
@@ -100,6 +103,7 @@ template <typename T>
 int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, bool fork, cudaEvent_t* ev);
 int launch_steps_direct(Ctx* ctx, int n, cudaStream_t s);
 int ensure_graph(Ctx* ctx);
+int check_guards(Ctx* ctx);
 size_t elem_size(const Ctx* ctx);
 
 }  // namespace ard

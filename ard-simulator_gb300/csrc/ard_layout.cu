@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <string>
@@ -565,7 +566,14 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   ARD_CUDA(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
   ARD_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
   ARD_CUDA(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
-  ARD_CUDA(cudaMalloc(&ctx->d_buf, std::max<size_t>(1, pool.off * es)));
+  // checked mode: 16 MiB sentinel guards on both sides of the pool catch stray writes
+  ctx->guard_bytes = ctx->debug_sync ? ((size_t)16 << 20) : 0;
+  ARD_CUDA(cudaMalloc(&ctx->d_buf_base, std::max<size_t>(1, pool.off * es) + 2 * ctx->guard_bytes));
+  ctx->d_buf = (char*)ctx->d_buf_base + ctx->guard_bytes;
+  if (ctx->guard_bytes) {
+    ARD_CUDA(cudaMemset(ctx->d_buf_base, 0xA5, ctx->guard_bytes));
+    ARD_CUDA(cudaMemset((char*)ctx->d_buf + pool.off * es, 0xA5, ctx->guard_bytes));
+  }
   ARD_CUDA(cudaMemset(ctx->d_buf, 0, pool.off * es));
   ARD_CUDA(cudaDeviceSynchronize());
   auto up = [&](auto** dptr, const auto& vec) -> int {
@@ -633,7 +641,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
 
 void free_ctx_device(Ctx* ctx) {
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
-  void* ptrs[] = {ctx->d_buf, ctx->d_mask, ctx->d_dct, ctx->d_pml, ctx->d_pml_blocks, ctx->d_ifs, ctx->d_srcpts,
+  void* ptrs[] = {ctx->d_buf_base, ctx->d_mask, ctx->d_dct, ctx->d_pml, ctx->d_pml_blocks, ctx->d_ifs, ctx->d_srcpts,
                   ctx->d_recpts, ctx->d_tiles, ctx->d_fwd1, ctx->d_fwd2, ctx->d_inv1, ctx->d_inv2, ctx->d_fwd2d,
                   ctx->d_inv2d, ctx->d_series,
                   ctx->d_hist, ctx->d_t};
@@ -645,6 +653,7 @@ void free_ctx_device(Ctx* ctx) {
   if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
   ctx->graph_exec = nullptr;
   ctx->d_buf = nullptr;
+  ctx->d_buf_base = nullptr;
 }
 
 // Dense 3D transform of one air partition, unpadded [d][h][w], from pool
@@ -883,3 +892,25 @@ extern "C" int ard_read_field(ard_ctx* c, int32_t scene, int32_t partition, floa
       }
   return ARD_OK;
 }
+
+namespace ard {
+// Checked mode: the guards around the pool must still hold their sentinel.
+int check_guards(Ctx* ctx) {
+  if (!ctx->guard_bytes) return ARD_OK;
+  std::vector<unsigned char> h(ctx->guard_bytes);
+  const size_t es = elem_size(ctx);
+  const char* sides[2] = {"before", "after"};
+  const char* addr[2] = {(const char*)ctx->d_buf_base, (const char*)ctx->d_buf + ctx->pool_elems * es};
+  for (int k = 0; k < 2; ++k) {
+    ARD_CUDA(cudaMemcpy(h.data(), addr[k], ctx->guard_bytes, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < h.size(); ++i)
+      if (h[i] != 0xA5) {
+        const long long off = k == 0 ? -(long long)(ctx->guard_bytes - i) : (long long)i;
+        ctx->err = std::string("stray write ") + sides[k] + " the element pool at byte offset " + std::to_string(off);
+        std::fprintf(stderr, "ard: %s\n", ctx->err.c_str());
+        return ARD_ERR_CUDA;
+      }
+  }
+  return ARD_OK;
+}
+}  // namespace ard
