@@ -315,8 +315,14 @@ class Simulation:
         return v.value
 
     def recorders(self, scene=0, t0=0, nt=None, f64=False):
+        """Recorder samples [nt][n_recorders]; scene=-1: every scene's recorders."""
         nt = self.time_step - t0 if nt is None else nt
-        nrec = self.scenes[scene].desc.n_recorders
+        if scene == -1:
+            nrec = sum(s.desc.n_recorders for s in self.scenes)
+        elif 0 <= scene < len(self.scenes):
+            nrec = self.scenes[scene].desc.n_recorders
+        else:
+            raise ArdError(6, f"bad scene index {scene}")
         if f64:
             out = np.zeros((nt, nrec), np.float64)
             self._c(lib().ard_read_recorders_f64(self._h, scene, out.ctypes.data_as(C.POINTER(C.c_double)), t0, nt))
@@ -326,6 +332,8 @@ class Simulation:
         return out
 
     def field(self, partition, scene=0):
+        if not (0 <= scene < len(self.scenes)) or not (0 <= partition < self.scenes[scene].desc.n_partitions):
+            raise ArdError(6, f"bad scene/partition index {scene}/{partition}")
         q = self.scenes[scene].partitions[partition]
         out = np.zeros((q[7], q[6], q[5]), np.float32)
         self._c(lib().ard_read_field(self._h, scene, partition, _fptr(out)))
