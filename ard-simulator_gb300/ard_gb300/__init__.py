@@ -100,6 +100,7 @@ SIGNATURES = {
     "ard_read_recorders": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.c_int64, C.c_int64]),
     "ard_read_recorders_f64": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int64, C.c_int64]),
     "ard_read_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
+    "ard_read_field_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float), C.c_void_p]),
     "ard_adjoint": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float),
                               C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "ard_read_initial_pressure_grad": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),

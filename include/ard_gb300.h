@@ -238,6 +238,19 @@ int ard_read_recorders_f64(ard_ctx* ctx, int32_t scene, double* out, int64_t t0,
  * partition this runs the full inverse transform of the current modes. */
 int ard_read_field(ard_ctx* ctx, int32_t scene, int32_t partition, float* out);
 
+/* No counterpart in the reference.  The field readout of ard_read_field for
+ * an air partition of an FP32 context, for callers that cannot allocate
+ * device memory: it allocates nothing.  The caller passes a device buffer of
+ * width*height*depth floats ([z][y][x]); the intermediate of the transform
+ * lives in a fixed device array inside the library (32 MiB, on every GPU that
+ * loads the library, until exit), so partitions are limited to 4,194,304
+ * cells and depth 1024 (ARD_ERR_RANGE beyond).  Asynchronous on `stream`
+ * (NULL: the context's stream), ordered after work already queued on the
+ * context.  The first call on a device looks up the array's device address
+ * and should come before any stream capture.  Calls share the array: calls
+ * whose work overlaps on the GPU race with each other. */
+int ard_read_field_noalloc(ard_ctx* ctx, int32_t scene, int32_t partition, float* out_device, void* stream);
+
 /* ---- adjoint (gradients of a recorder misfit) ---- */
 
 /* Gradients of J = 0.5 * sum_{t<T} sum_r w_r (rec[t][r] - target[t][r])^2
