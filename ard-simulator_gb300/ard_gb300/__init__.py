@@ -74,7 +74,8 @@ class SceneParams(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("max_steps", C.c_int64), ("use_graphs", C.c_int32),
-                ("device", C.c_int32), ("autotune", C.c_int32), ("arithmetic", C.c_int32)]
+                ("device", C.c_int32), ("autotune", C.c_int32), ("arithmetic", C.c_int32),
+                ("adjoint", C.c_int32)]
 
 
 # Every exported symbol with its ctypes signature (checked against the header by the tests).
@@ -247,13 +248,13 @@ class Simulation:
     """Context over one or many scenes (many = batched mode)."""
 
     def __init__(self, scenes, precision=PREC_F32, max_steps=4096, use_graphs=True, device=0,
-                 arithmetic=ARITH_ACCURATE):
+                 arithmetic=ARITH_ACCURATE, adjoint=False):
         if isinstance(scenes, Scene):
             scenes = [scenes]
         self.scenes = list(scenes)
         arr = (SceneDesc * len(self.scenes))(*[s.desc for s in self.scenes])
         self._arr = arr
-        opt = Options(precision, max_steps, 1 if use_graphs else 0, device, 0, arithmetic)
+        opt = Options(precision, max_steps, 1 if use_graphs else 0, device, 0, arithmetic, 1 if adjoint else 0)
         h = C.c_void_p()
         _check(lib().ard_create(arr, len(self.scenes), C.byref(opt), C.byref(h)))
         self._h = h
@@ -330,6 +331,33 @@ class Simulation:
         else:
             out = np.zeros((nt, nrec), np.float32)
             self._c(lib().ard_read_recorders(self._h, scene, _fptr(out), t0, nt))
+        return out
+
+    def adjoint(self, T, target, checkpoint_every=0, want_scale=True):
+        """Gradients of J = 0.5 sum_{t<T} sum_r (rec[t][r] - target[t][r])^2 per scene
+        (ard_adjoint).  `target`: [T][n_recorders] for one scene, or a list of
+        such arrays, one per scene.  Runs the forward from step 0 itself.
+        Returns dict(loss [n_scenes], grad_source [n_sources_total][T],
+        grad_scale [n_scenes][6] or None)."""
+        parts = target if isinstance(target, (list, tuple)) else [target]
+        if len(parts) != len(self.scenes):
+            raise ArdError(1, "one target array per scene")
+        tg = np.concatenate([np.ascontiguousarray(t, np.float32).reshape(T, -1).ravel() for t in parts])
+        nsrc = sum(s.desc.n_sources for s in self.scenes)
+        gsrc = np.zeros((max(nsrc, 1), T), np.float32)
+        gsc = np.zeros((len(self.scenes), 6), np.float32) if want_scale else None
+        loss = np.zeros(len(self.scenes), np.float32)
+        self._c(lib().ard_adjoint(self._h, T, _fptr(tg), checkpoint_every, _fptr(gsrc),
+                                  _fptr(gsc) if want_scale else None, _fptr(loss)))
+        return {"loss": loss, "grad_source": gsrc[:nsrc], "grad_scale": gsc}
+
+    def initial_pressure_grad(self, partition, scene=0):
+        """dJ/d(initial pressure) of an air partition after adjoint(), [z][y][x]."""
+        if not (0 <= scene < len(self.scenes)) or not (0 <= partition < self.scenes[scene].desc.n_partitions):
+            raise ArdError(6, f"bad scene/partition index {scene}/{partition}")
+        q = self.scenes[scene].partitions[partition]
+        out = np.zeros((q[7], q[6], q[5]), np.float32)
+        self._c(lib().ard_read_initial_pressure_grad(self._h, scene, partition, _fptr(out)))
         return out
 
     def field(self, partition, scene=0):

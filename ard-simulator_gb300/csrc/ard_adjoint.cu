@@ -1,21 +1,404 @@
-// Adjoint of the ARD time step (gradients of a recorder misfit).
+// Adjoint of the ARD time step: gradients of the recorder misfit
+//   J = 0.5 sum_{t < T} sum_r (rec[t][r] - target[t][r])^2
+// with respect to the source series, the initial pressure of the air
+// partitions and the per-face PML damping scales.
+//
+// The step is linear in its state (modal levels, shell forces, PML fields),
+// so the adjoint recursion needs no forward state except for the damping
+// gradient, whose terms multiply forward PML values.  Without that gradient
+// the call is one forward run (recorder residuals) and one backward run.
+// With it, the forward run stores a copy of the state block every K steps;
+// the backward run then works through the segments last to first, each one
+// recomputed from its checkpoint while the PML pressure and phi_n of every
+// step are kept, then swept backwards.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <string>
+#include <vector>
 
+#include "ard_adjoint_kernels.cuh"
 #include "ard_engine.h"
 #include "ard_gb300.h"
+#include "ard_kernels.cuh"
 
 using namespace ard;
 
-extern "C" int ard_adjoint(ard_ctx* c, int64_t, const float*, int32_t, float*, float*, float*) {
-  if (!c) return ARD_ERR_INVALID;
-  reinterpret_cast<Ctx*>(c)->err = "ard_adjoint: not available in this build";
-  return ARD_ERR_STATE;
+#define ARD_CUDA(call)                                                                                   \
+  do {                                                                                                   \
+    cudaError_t e_ = (call);                                                                             \
+    if (e_ != cudaSuccess) {                                                                             \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorName(e_) + " (" + cudaGetErrorString(e_) + ")"; \
+      return e_ == cudaErrorMemoryAllocation ? ARD_ERR_OOM : ARD_ERR_CUDA;                               \
+    }                                                                                                    \
+  } while (0)
+
+namespace {
+
+int grid_for(long long work, int per_block, int max_blocks) {
+  long long b = (work + per_block - 1) / per_block;
+  if (b < 1) b = 1;
+  if (b > max_blocks) b = max_blocks;
+  return (int)b;
 }
 
-extern "C" int ard_read_initial_pressure_grad(ard_ctx* c, int32_t, int32_t, float*) {
+// Device buffers of one ard_adjoint call.
+struct AdjBuffers {
+  void* resid = nullptr;      // [T][n_rec_total] residuals (context precision)
+  double* gsrc = nullptr;     // [T][n_src_total]
+  double* gz = nullptr;       // [pml blocks][kMaxPmlLayers]
+  void* ckpt = nullptr;       // [n_ckpt + 1][state] (last: the state after step T)
+  void* hist_p = nullptr;     // [K + 1][region]
+  void* hist_phn = nullptr;   // [K][region]
+  ~AdjBuffers() {
+    void* ptrs[] = {resid, gsrc, gz, ckpt, hist_p, hist_phn};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+  }
+};
+
+// Launch attributes of the kernels launched from this file.
+template <typename T>
+int configure_adjoint(Ctx* ctx) {
+  const int msmem = (int)(kModalSmemElems * sizeof(T));
+  ARD_CUDA(cudaFuncSetAttribute(modal_kernel<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, msmem));
+  ARD_CUDA(cudaFuncSetAttribute(modal_kernel<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, msmem));
+  if (ctx->fused_faces)
+    ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->f2d_bytes));
+  return ARD_OK;
+}
+
+struct HistView {
+  const void* p = nullptr;
+  const void* phn = nullptr;
+  long long hlen = 0;
+  double* gz = nullptr;
+};
+
+// One adjoint step t (tstep: position inside the launch sequence, counted
+// backwards from the counter d_tb[0]).
+template <typename T>
+int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t s2, const AdjBuffers& ab,
+                        const HistView& hv) {
+  T* buf = reinterpret_cast<T*>(ctx->d_buf);
+  const int lout = t % 3, lin = (t + 1) % 3, ly = (t + 2) % 3;
+  const int par = t & 1;
+  if (ctx->q_end > ctx->q_begin)
+    ARD_CUDA(cudaMemsetAsync(buf + ctx->q_begin, 0, sizeof(T) * (size_t)(ctx->q_end - ctx->q_begin), s));
+  if (ctx->n_face_cells > 0) {
+    IfaceAdjArgs<T> ia{buf, ctx->d_ifs, (int)ctx->ifs.size(), ctx->n_face_cells, ctx->d_dct, ctx->d_pml,
+                       ctx->d_mask, lin, lout, (T)ctx->c0, (T)ctx->dh, (T)ctx->dt};
+    iface_adjoint_kernel<T><<<grid_for(ctx->n_face_cells, 256, ctx->num_sms * 16), 256, 0, s>>>(ia);
+    ARD_CUDA(cudaGetLastError());
+  }
+  const bool fork = !ctx->pml_blocks.empty() && !ctx->dct.empty();
+  if (fork) {
+    ARD_CUDA(cudaEventRecord(ctx->ev_fork, s));
+    ARD_CUDA(cudaStreamWaitEvent(s2, ctx->ev_fork, 0));
+  }
+  if (!ctx->pml_blocks.empty()) {
+    PmlAdjArgs<T> pa{buf, ctx->d_pml, ctx->d_pml_blocks, (int)ctx->pml_blocks.size(), lin, ly, lout, (t + 1) & 1,
+                     (T)ctx->dt, (T)ctx->dh, (T)ctx->c0, (const T*)hv.p, (const T*)hv.phn, hv.hlen, ctx->d_tb,
+                     tstep, hv.gz};
+    pml_adjoint_kernel<T><<<grid_for((long long)ctx->pml_blocks.size(), 1, ctx->num_sms * 8), 256, 0,
+                            fork ? s2 : s>>>(pa);
+    ARD_CUDA(cudaGetLastError());
+  }
+  if (!ctx->dct.empty()) {
+    const int gx = ctx->num_sms * 4;
+    if (ctx->fused_faces) {
+      face2d_kernel<T><<<grid_for((long long)ctx->adj1_2d.size(), 1, gx), 256, ctx->f2d_bytes, s>>>(
+          buf, ctx->d_adj1_2d, (int)ctx->adj1_2d.size(), ctx->f2d_smem);
+    } else {
+      for (int k = 0; k < 2; ++k)
+        xform_gemm_kernel<T><<<grid_for(ctx->adjg[k].units, 1, gx), 256, 0, s>>>(
+            buf, ctx->d_adjg[k], (int)ctx->adjg[k].jobs.size(), ctx->adjg[k].units);
+    }
+    ARD_CUDA(cudaGetLastError());
+    ModalArgs<T> ma{buf, ctx->d_dct, ctx->d_tiles, (int)ctx->tiles.size(), ctx->d_srcpts, ctx->d_recpts,
+                    ctx->d_series, ctx->max_steps, ctx->d_tb, tstep, par, (const T*)ab.resid, ctx->n_rec_total};
+    const size_t msmem = kModalSmemElems * sizeof(T);
+    const int mgrid = grid_for((long long)ctx->tiles.size(), 1, ctx->num_sms * 2);
+    if (ctx->arith == ARD_ARITH_REFERENCE)
+      modal_kernel<T, true, true><<<mgrid, kModalThreads, msmem, s>>>(ma);
+    else
+      modal_kernel<T, false, true><<<mgrid, kModalThreads, msmem, s>>>(ma);
+    ARD_CUDA(cudaGetLastError());
+    if (!ctx->srcpts.empty()) {
+      srcgrad_kernel<T><<<grid_for((long long)ctx->srcpts.size() * 32, 128, 1 << 30), 128, 0, s>>>(
+          buf, ctx->d_dct, ctx->d_srcpts, (int)ctx->srcpts.size(), ctx->n_src_total, ab.gsrc, ctx->d_tb, tstep);
+      ARD_CUDA(cudaGetLastError());
+    }
+    if (ctx->fused_faces) {
+      face2d_kernel<T><<<grid_for((long long)ctx->adj2_2d.size(), 1, gx), 256, ctx->f2d_bytes, s>>>(
+          buf, ctx->d_adj2_2d, (int)ctx->adj2_2d.size(), ctx->f2d_smem);
+    } else {
+      for (int k = 2; k < 4; ++k)
+        xform_gemm_kernel<T><<<grid_for(ctx->adjg[k].units, 1, gx), 256, 0, s>>>(
+            buf, ctx->d_adjg[k], (int)ctx->adjg[k].jobs.size(), ctx->adjg[k].units);
+    }
+    ARD_CUDA(cudaGetLastError());
+  }
+  if (fork) {
+    ARD_CUDA(cudaEventRecord(ctx->ev_join, s2));
+    ARD_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+  }
+  if (ctx->debug_sync) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      ctx->err = std::string("adjoint step ") + std::to_string(t) + ": " + cudaGetErrorString(e);
+      return ARD_ERR_CUDA;
+    }
+  }
+  return ARD_OK;
+}
+
+// Adjoint steps t_hi - 1 down to t_lo.
+template <typename T>
+int run_backward(Ctx* ctx, long long t_hi, long long t_lo, long long hist_t0, const AdjBuffers& ab,
+                 const HistView& hv) {
+  cudaStream_t s = ctx->stream;
+  set_counters_kernel<<<1, 32, 0, s>>>(ctx->d_tb, t_hi - 1, hist_t0);
+  ARD_CUDA(cudaGetLastError());
+  for (long long t = t_hi - 1; t >= t_lo; --t) {
+    int rc = launch_adjoint_step<T>(ctx, (int)t, (int)(t_hi - 1 - t), s, ctx->stream2, ab, hv);
+    if (rc) return rc;
+  }
+  return ARD_OK;
+}
+
+static __global__ void set_step_counter_kernel(long long* tcount, long long v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *tcount = v;
+}
+
+template <typename T>
+int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoint_every, float* grad_source,
+                 float* grad_scale, float* loss) {
+  const size_t es = sizeof(T);
+  cudaStream_t s = ctx->stream;
+  int rc = configure_adjoint<T>(ctx);
+  if (rc) return rc;
+  const bool need_hist = grad_scale != nullptr && !ctx->pml.empty();
+  const long long state_len = ctx->state_end - ctx->state_begin;
+  const long long hlen = ctx->pml_region[0][1] - ctx->pml_region[0][0];
+  long long K = T_steps, n_ckpt = 1;
+  bool use_ckpt = false;
+  AdjBuffers ab;
+  if (need_hist) {
+    size_t free_b = 0, total_b = 0;
+    ARD_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t full = (size_t)(2 * T_steps + 1) * hlen * es;
+    if (checkpoint_every > 0) {
+      K = std::min<long long>(checkpoint_every, T_steps);
+      use_ckpt = true;
+    } else if (full > free_b / 2) {
+      // balance checkpoint memory (n_ckpt states) against history memory (2 K PML regions)
+      const double k = std::sqrt((double)T_steps * (double)state_len / (2.0 * (double)std::max(1LL, hlen)));
+      K = std::max(1LL, std::min(T_steps, (long long)std::ceil(k)));
+      use_ckpt = true;
+    }
+    n_ckpt = (T_steps + K - 1) / K;
+    const size_t need = (use_ckpt ? (size_t)(n_ckpt + 1) * state_len * es : 0) + (size_t)(2 * K + 1) * hlen * es;
+    if (need > free_b / 10 * 9) {
+      ctx->err = "ard_adjoint: checkpoints and PML history need " + std::to_string(need >> 20) + " MiB (" +
+                 std::to_string(n_ckpt) + " checkpoints every " + std::to_string(K) + " steps); " +
+                 std::to_string(free_b >> 20) + " MiB free";
+      return ARD_ERR_OOM;
+    }
+    if (use_ckpt) ARD_CUDA(cudaMalloc(&ab.ckpt, (size_t)(n_ckpt + 1) * state_len * es));
+    ARD_CUDA(cudaMalloc(&ab.hist_p, (size_t)(K + 1) * hlen * es));
+    ARD_CUDA(cudaMalloc(&ab.hist_phn, (size_t)K * hlen * es));
+  }
+  const int nrec = ctx->n_rec_total, nsrc = ctx->n_src_total;
+  ARD_CUDA(cudaMalloc(&ab.resid, std::max<size_t>(1, (size_t)T_steps * nrec * es)));
+  ARD_CUDA(cudaMalloc(&ab.gsrc, std::max<size_t>(1, (size_t)T_steps * nsrc * sizeof(double))));
+  ARD_CUDA(cudaMalloc(&ab.gz, std::max<size_t>(1, ctx->pml_blocks.size() * kMaxPmlLayers * sizeof(double))));
+  ARD_CUDA(cudaMemsetAsync(ab.gsrc, 0, (size_t)T_steps * nsrc * sizeof(double), s));
+  ARD_CUDA(cudaMemsetAsync(ab.gz, 0, ctx->pml_blocks.size() * kMaxPmlLayers * sizeof(double), s));
+
+  T* buf = reinterpret_cast<T*>(ctx->d_buf);
+  T* state = buf + ctx->state_begin;
+  auto ckpt = [&](long long i) { return reinterpret_cast<T*>(ab.ckpt) + i * state_len; };
+
+  // The PML kernel keeps p(t) and phi_n(t) of steps t0 <= t < t1 (the slot
+  // of p(t0 - 1) is filled here from the state before step t0).
+  T* hp = reinterpret_cast<T*>(ab.hist_p);
+  T* hphn = reinterpret_cast<T*>(ab.hist_phn);
+  auto keep_history = [&](long long t0, long long t1) -> int {
+    PmlHist<T> h{hp, hphn, hlen, t0, t1};
+    const int q_prev = (int)((t0 + 1) & 1);   // level of p(t0 - 1)
+    ARD_CUDA(cudaMemcpyAsync(hp, buf + ctx->pml_region[q_prev][0], hlen * es, cudaMemcpyDeviceToDevice, s));
+    ARD_CUDA(cudaMemcpyAsync(ctx->d_phist, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    return ARD_OK;
+  };
+  auto stop_history = [&]() -> int {
+    PmlHist<T> h{nullptr, nullptr, 0, 0, 0};
+    ARD_CUDA(cudaMemcpyAsync(ctx->d_phist, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    return ARD_OK;
+  };
+
+  // ---- forward run: keeps the whole PML history, or a checkpoint at the start of every segment ----
+  ard_ctx* handle = reinterpret_cast<ard_ctx*>(ctx);
+  if (use_ckpt) {
+    for (long long i = 0; i < n_ckpt; ++i) {
+      ARD_CUDA(cudaMemcpyAsync(ckpt(i), state, state_len * es, cudaMemcpyDeviceToDevice, s));
+      rc = ard_step(handle, std::min(K, T_steps - i * K), nullptr);
+      if (rc) return rc;
+    }
+    ARD_CUDA(cudaMemcpyAsync(ckpt(n_ckpt), state, state_len * es, cudaMemcpyDeviceToDevice, s));
+  } else {
+    if (need_hist && (rc = keep_history(0, T_steps))) return rc;
+    rc = ard_step(handle, T_steps, nullptr);
+    if (rc) return rc;
+    if (need_hist && (rc = stop_history())) return rc;
+  }
+
+  // ---- residuals and misfit ----
+  ARD_CUDA(cudaStreamSynchronize(s));
+  std::vector<double> rec((size_t)T_steps * nrec);
+  if (nrec > 0)
+    ARD_CUDA(cudaMemcpy(rec.data(), ctx->d_hist, rec.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  std::vector<T> res(rec.size());
+  std::vector<double> scene_loss(ctx->scenes.size(), 0.0);
+  for (size_t si = 0; si < ctx->scenes.size(); ++si) {
+    const SceneRec& sr = ctx->scenes[si];
+    for (long long t = 0; t < T_steps; ++t)
+      for (int r = 0; r < sr.nrec; ++r) {
+        const int g = sr.rec0 + r;
+        // target rows are concatenated over scenes: scene si's block is T x nrec(si)
+        const double tg = target[(size_t)sr.rec0 * T_steps + (size_t)t * sr.nrec + r];
+        const double e = rec[(size_t)t * nrec + g] - tg;
+        res[(size_t)t * nrec + g] = (T)e;
+        scene_loss[si] += 0.5 * e * e;
+      }
+  }
+  if (nrec > 0)
+    ARD_CUDA(cudaMemcpy(ab.resid, res.data(), res.size() * es, cudaMemcpyHostToDevice));
+
+  // ---- backward run ----
+  const long long adj_len = ctx->adj_end - ctx->adj_begin;
+  ARD_CUDA(cudaMemsetAsync(buf + ctx->adj_begin, 0, adj_len * es, s));
+  const HistView hv = need_hist ? HistView{ab.hist_p, ab.hist_phn, hlen, ab.gz} : HistView{};
+  if (use_ckpt) {
+    for (long long i = n_ckpt - 1; i >= 0; --i) {
+      const long long t0 = i * K, t1 = std::min(T_steps, t0 + K);
+      // run the segment again from its checkpoint, keeping its PML history
+      ARD_CUDA(cudaMemcpyAsync(state, ckpt(i), state_len * es, cudaMemcpyDeviceToDevice, s));
+      set_step_counter_kernel<<<1, 32, 0, s>>>(ctx->d_t, t0);
+      ARD_CUDA(cudaGetLastError());
+      ctx->t_host = t0;
+      if ((rc = keep_history(t0, t1))) return rc;
+      rc = ard_step(handle, t1 - t0, nullptr);
+      if (rc) return rc;
+      if ((rc = stop_history())) return rc;
+      rc = run_backward<T>(ctx, t1, t0, t0, ab, hv);
+      if (rc) return rc;
+    }
+    // leave the forward state as after step T
+    ARD_CUDA(cudaMemcpyAsync(state, ckpt(n_ckpt), state_len * es, cudaMemcpyDeviceToDevice, s));
+    set_step_counter_kernel<<<1, 32, 0, s>>>(ctx->d_t, T_steps);
+    ARD_CUDA(cudaGetLastError());
+    ctx->t_host = T_steps;
+  } else {
+    rc = run_backward<T>(ctx, T_steps, 0, 0, ab, hv);
+    if (rc) return rc;
+  }
+  ARD_CUDA(cudaStreamSynchronize(s));
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream2));
+
+  // ---- outputs ----
+  if (grad_source && nsrc > 0) {
+    std::vector<double> g((size_t)T_steps * nsrc);
+    ARD_CUDA(cudaMemcpy(g.data(), ab.gsrc, g.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    // [source][t], sources numbered scene by scene (the layout of the source series)
+    for (int q = 0; q < nsrc; ++q)
+      for (long long t = 0; t < T_steps; ++t) grad_source[(size_t)q * T_steps + t] = (float)g[(size_t)t * nsrc + q];
+  }
+  if (grad_scale) {
+    for (size_t si = 0; si < ctx->scenes.size(); ++si)
+      for (int f = 0; f < 6; ++f) grad_scale[si * 6 + f] = 0.f;
+    if (need_hist) {
+      std::vector<double> gz(ctx->pml_blocks.size() * kMaxPmlLayers);
+      ARD_CUDA(cudaMemcpy(gz.data(), ab.gz, gz.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      std::vector<std::vector<double>> per_slab(ctx->pml.size());
+      for (size_t k = 0; k < ctx->pml.size(); ++k) per_slab[k].assign(ctx->pml[k].L, 0.0);
+      for (size_t b = 0; b < ctx->pml_blocks.size(); ++b) {
+        const int slab = ctx->pml_blocks[b].x;
+        for (int l = 0; l < ctx->pml[slab].L; ++l) per_slab[slab][l] += gz[b * kMaxPmlLayers + l];
+      }
+      std::vector<double> acc(ctx->scenes.size() * 6, 0.0);
+      for (size_t k = 0; k < ctx->pml.size(); ++k) {
+        const PmlDev& P = ctx->pml[k];
+        std::vector<double> z0;
+        pml_profile_unit(ctx, P.type, P.L, &z0);
+        for (int l = 0; l < P.L; ++l) acc[(size_t)P.scene * 6 + P.type] += per_slab[k][l] * z0[l];
+      }
+      for (size_t i = 0; i < acc.size(); ++i) grad_scale[i] = (float)acc[i];
+    }
+  }
+  if (loss)
+    for (size_t si = 0; si < ctx->scenes.size(); ++si) loss[si] = (float)scene_loss[si];
+  ctx->adj_valid = true;
+  return ARD_OK;
+}
+
+}  // namespace
+
+extern "C" int ard_adjoint(ard_ctx* c, int64_t T, const float* target, int32_t checkpoint_every, float* grad_source,
+                           float* grad_scale, float* loss) {
   if (!c) return ARD_ERR_INVALID;
-  reinterpret_cast<Ctx*>(c)->err = "ard_read_initial_pressure_grad: not available in this build";
-  return ARD_ERR_STATE;
+  Ctx* ctx = reinterpret_cast<Ctx*>(c);
+  if (!ctx->adjoint) { ctx->err = "ard_adjoint: context created without options.adjoint"; return ARD_ERR_STATE; }
+  if (T < 1 || T > ctx->max_steps) { ctx->err = "ard_adjoint: T must be in [1, max_steps]"; return ARD_ERR_RANGE; }
+  if (ctx->n_rec_total > 0 && !target) { ctx->err = "ard_adjoint: target is NULL"; return ARD_ERR_INVALID; }
+  if (ctx->t_host != 0) {
+    ctx->err = "ard_adjoint: runs the forward from step 0 (call ard_reset, then set the initial pressure)";
+    return ARD_ERR_STATE;
+  }
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  ctx->adj_valid = false;
+  return ctx->prec == ARD_PREC_F64
+             ? adjoint_impl<double>(ctx, T, target, checkpoint_every, grad_source, grad_scale, loss)
+             : adjoint_impl<float>(ctx, T, target, checkpoint_every, grad_source, grad_scale, loss);
+}
+
+extern "C" int ard_read_initial_pressure_grad(ard_ctx* c, int32_t scene, int32_t partition, float* out) {
+  if (!c || !out) return ARD_ERR_INVALID;
+  Ctx* ctx = reinterpret_cast<Ctx*>(c);
+  if (!ctx->adj_valid) { ctx->err = "ard_read_initial_pressure_grad: no adjoint run since the last reset"; return ARD_ERR_STATE; }
+  if (scene < 0 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
+  const SceneRec& sr = ctx->scenes[scene];
+  if (partition < 0 || partition >= (int)sr.parts.size()) { ctx->err = "bad partition index"; return ARD_ERR_RANGE; }
+  if (sr.parts[partition].kind != ARD_PART_DCT) {
+    ctx->err = "initial pressure applies to air partitions";
+    return ARD_ERR_INVALID;
+  }
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  const DctDev& D = ctx->dct[sr.engine_idx[partition]];
+  const long long N = (long long)D.w * D.h * D.d;
+  const long long s0 = ctx->scratch;
+  const int blocks = (int)std::min<long long>((N + 255) / 256, 8192);
+  // the modes are m0 = kappa C^3 p0 with kappa = 1 / (8 N s_i); dJ/dp0 = kappa (C^T)^3 dJ/dm0
+  const double kappa = 1.0 / (8.0 * (double)N / std::sqrt(2.0 * (double)N));
+  int rc;
+  if (ctx->prec == ARD_PREC_F64) {
+    if (ctx->arith == ARD_ARITH_REFERENCE) init_grad_kernel<double, true><<<blocks, 256, 0, ctx->stream>>>((double*)ctx->d_buf, D, s0 + N);
+    else init_grad_kernel<double, false><<<blocks, 256, 0, ctx->stream>>>((double*)ctx->d_buf, D, s0 + N);
+    ARD_CUDA(cudaGetLastError());
+    rc = dense_transform_ex<double>(ctx, D, s0 + N, s0 + N, s0, 0, true, kappa);
+    if (rc) return rc;
+    std::vector<double> h((size_t)N);
+    ARD_CUDA(cudaMemcpy(h.data(), (double*)ctx->d_buf + s0 + N, N * sizeof(double), cudaMemcpyDeviceToHost));
+    for (long long i = 0; i < N; ++i) out[i] = (float)h[i];
+  } else {
+    if (ctx->arith == ARD_ARITH_REFERENCE) init_grad_kernel<float, true><<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, D, s0 + N);
+    else init_grad_kernel<float, false><<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, D, s0 + N);
+    ARD_CUDA(cudaGetLastError());
+    rc = dense_transform_ex<float>(ctx, D, s0 + N, s0 + N, s0, 0, true, kappa);
+    if (rc) return rc;
+    ARD_CUDA(cudaMemcpy(out, (float*)ctx->d_buf + s0 + N, N * sizeof(float), cudaMemcpyDeviceToHost));
+  }
+  return ARD_OK;
 }

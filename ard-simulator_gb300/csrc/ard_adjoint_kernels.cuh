@@ -1,0 +1,359 @@
+// sm_103a kernels of the adjoint ARD step (gradients of a recorder misfit).
+//
+// The forward step is linear in its state, so the adjoint runs the
+// transposed step backwards in time.  Per adjoint step t (after the forward
+// step t's adjoint variables of step t + 1 are known):
+//   iface_adjoint_kernel   transposed interface forcing: the adjoint shell
+//                          force and PML strip force -> adjoint face pressure
+//                          and adjoint PML pressure (atomic accumulation)
+//   pml_adjoint_kernel     transposed Grote-Sim update; accumulates the
+//                          gradient of every damping layer zeta(l) from the
+//                          forward PML history
+//   face2d / GEMM jobs     adjoint of the inverse face transform
+//   modal_kernel<ADJ>      transposed modal recurrence, recorder residual
+//                          injection, source-series gradient partials
+//   srcgrad_kernel         source-series gradient of step t
+//   face2d / GEMM jobs     adjoint of the forward face transform -> adjoint
+//                          shell force of step t - 1
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ard_device.cuh"
+#include "ard_kernels.cuh"
+
+namespace ard {
+
+// ---------------------------------------------------------------------------
+// Interface forcing, transposed
+// ---------------------------------------------------------------------------
+
+template <typename T>
+struct IfaceAdjArgs {
+  T* buf;
+  const IfaceDev* ifs;
+  int nif;
+  long long total;
+  const DctDev* dct;
+  const PmlDev* pml;
+  const unsigned char* masks;
+  int lin;    // level of the adjoint PML pressure of step t + 1 (the strip force enters p(t + 1) times dt^2)
+  int lout;   // level of the adjoint PML pressure of step t (accumulated)
+  T c0, dh, dt;
+};
+
+// Adjoint of the force value that the forward step writes at crossing
+// coordinate c, face coordinates (u, v) of side s.
+template <typename T>
+__device__ __forceinline__ T adj_force(const IfaceAdjArgs<T>& a, int type, const SideDev& s, int c, int u, int v) {
+  if (s.kind == 0) {
+    const DctDev& D = a.dct[s.idx];
+    const int x = type == 0 ? c : u;
+    const int y = type == 0 ? u : (type == 1 ? c : v);
+    const int z = type == 2 ? c : v;
+    const long long o = shell_index(D, x, y, z);
+    return o >= 0 ? a.buf[o - D.fX + D.aX] : (T)0;
+  }
+  const PmlDev& P = a.pml[s.idx];
+  return a.dt * a.dt * a.buf[P.ap[a.lin] + ((long long)c * P.A + v) * P.B + u];
+}
+
+template <typename T>
+__device__ __forceinline__ void adj_pressure_add(const IfaceAdjArgs<T>& a, int type, const SideDev& s, int c, int u,
+                                                 int v, T val) {
+  if (val == (T)0) return;
+  if (s.kind == 0) {
+    const DctDev& D = a.dct[s.idx];
+    const int layer = face_layer(c, s.ext);
+    long long o;
+    if (type == 0) o = D.qX + ((long long)layer * D.d + v) * D.h + u;
+    else if (type == 1) o = D.qY + ((long long)layer * D.d + v) * D.wp + u;
+    else o = D.qZ + ((long long)layer * D.h + v) * D.wp + u;
+    atomicAdd(a.buf + o, val);
+    return;
+  }
+  const PmlDev& P = a.pml[s.idx];
+  atomicAdd(a.buf + P.ap[a.lout] + ((long long)c * P.A + v) * P.B + u, val);
+}
+
+// Transpose of iface_kernel: every force value the forward step writes
+// (mask bit set) sends its adjoint back through the same 6-point stencil to
+// the three pressure layers on each side that it was computed from.
+template <typename T>
+__global__ void __launch_bounds__(256) iface_adjoint_kernel(IfaceAdjArgs<T> a) {
+  const T C[6][6] = {{0, 0, -2, 2, 0, 0},       {0, -2, 27, -27, 2, 0},     {-2, 27, -270, 270, -27, 2},
+                     {2, -27, 270, -270, 27, -2}, {0, 2, -27, 27, -2, 0},     {0, 0, 2, -2, 0, 0}};
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < a.total;
+       g += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = a.nif - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (a.ifs[mid].cell0 <= g) lo = mid; else hi = mid - 1;
+    }
+    const IfaceDev& I = a.ifs[lo];
+    const long long local = g - I.cell0;
+    const int nu = I.u1 - I.u0;
+    const int iu = I.u0 + (int)(local % nu);
+    const int iv = I.v0 + (int)(local / nu);
+    const unsigned mask = a.masks[I.mask + local];
+    const int lu = iu - I.lo.ou, lv = iv - I.lo.ov;
+    const int hu = iu - I.hi.ou, hv = iv - I.hi.ov;
+    const T k = (T)I.absorption * (a.c0 * a.c0) / ((T)180 * a.dh * a.dh);
+    T gl[3] = {0, 0, 0}, gh[3] = {0, 0, 0};
+#pragma unroll
+    for (int m = -3; m < 3; ++m) {
+      if (!(mask & (1u << (m + 3)))) continue;
+      const T fb = m < 0 ? adj_force(a, I.type, I.lo, I.lo.ext + m, lu, lv) : adj_force(a, I.type, I.hi, m, hu, hv);
+      const T g = k * fb;
+      const bool use_lo = m < 0 ? I.lo.self != 0 : true;
+      const bool use_hi = m < 0 ? true : I.hi.self != 0;
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        if (use_lo) gl[n] += g * C[m + 3][n];
+        if (use_hi) gh[n] += g * C[m + 3][3 + n];
+      }
+    }
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      adj_pressure_add(a, I.type, I.lo, I.lo.ext - 3 + n, lu, lv, gl[n]);
+      adj_pressure_add(a, I.type, I.hi, n, hu, hv, gh[n]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// PML, transposed
+// ---------------------------------------------------------------------------
+
+template <typename T>
+struct PmlAdjArgs {
+  T* buf;
+  const PmlDev* pml;
+  const int4* blocks;   // {slab, a0, b0}: the forward kernel's 8 x 32 plane tiles
+  int nblocks;
+  int lx, ly, lo;       // adjoint pressure levels of steps t + 1, t + 2 (read, then cleared) and t (accumulated)
+  int fin;              // level of the adjoint phi of step t + 1; step t's goes to fin ^ 1
+  T dt, dh, c0;
+  // forward PML history for the damping gradient (null: no gradient):
+  // hist_p[j] = p(t0 - 1 + j), hist_phn[j] = phi_n(t0 + j), each `hlen`
+  // elements in the all-slab region layout (slab at PmlDev::hoff)
+  const T* hist_p;
+  const T* hist_phn;
+  long long hlen;
+  const long long* tc;  // {t of the first step of the launch sequence, t0}
+  int tstep;
+  double* gz;           // [nblocks][kMaxPmlLayers] damping-gradient sums (accumulated)
+};
+
+// With X = adjoint p(t+1), Y = adjoint p(t+2), Phi = adjoint phi(t+1) and
+// the forward operators of pml_kernel (L: 7-point Laplacian, D: 5-point
+// derivative; L^T = L and D^T = -D under the zero-outside-the-slab rule):
+//   p~(t)    += 2 X + dt^2 c^2 L X - dt z X + (-1 + dt z) Y
+//               + dt Dn(z Phi_n) - dt z (Da Phi_a + Db Phi_b)
+//   phi~n(t)  = (1 - dt z) Phi_n - dt^2 Dn X
+//   phi~a(t)  = Phi_a - dt^2 Da X,   phi~b(t) = Phi_b - dt^2 Db X
+// and, from the forward p(t), p(t-1), phi_n(t), the derivative of the
+// forward step t + 1 with respect to z(l):
+//   dJ/dz(l) += sum over layer l of  -dt X (p(t) - p(t-1))
+//               - dt Phi_n (phi_n(t) + Dn p(t)) + dt Phi_a Da p(t) + dt Phi_b Db p(t)
+template <typename T>
+__global__ void __launch_bounds__(256) pml_adjoint_kernel(PmlAdjArgs<T> a) {
+  constexpr int TA = 8, TB = 32;
+  __shared__ T Xs[TA + 6][TB + 6];
+  __shared__ T FA[TA + 4][TB];
+  __shared__ T FB[TA][TB + 4];
+  __shared__ T Qs[TA + 4][TB + 4];
+  __shared__ double red[8][kMaxPmlLayers];
+  const T c7[7] = {2, -27, 270, -490, 270, -27, 2};
+  const T c5[5] = {1, -8, 0, 8, -1};
+  const int tb = threadIdx.x & 31, ta = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool zgrad = a.hist_p != nullptr;
+  long long hofs = 0;
+  if (zgrad) {
+    const long long t = a.tc[0] - a.tstep;
+    hofs = t - a.tc[1];   // hist_p[hofs + 1] = p(t), hist_p[hofs] = p(t-1), hist_phn[hofs] = phi_n(t)
+  }
+  const T dt = a.dt, dt2 = a.dt * a.dt;
+  for (int bi = blockIdx.x; bi < a.nblocks; bi += gridDim.x) {
+    const int4 blk = a.blocks[bi];
+    const PmlDev& P = a.pml[blk.x];
+    const int L = P.L, A = P.A, B = P.B;
+    const int a0 = blk.y, b0 = blk.z;
+    const int ia = a0 + ta, ib = b0 + tb;
+    const bool inside = ia < A && ib < B;
+    const long long lstride = (long long)A * B;
+    const long long col = inside ? (long long)ia * B + ib : 0;
+    const T* X = a.buf + P.ap[a.lx];
+    T* Y = a.buf + P.ap[a.ly];
+    T* O = a.buf + P.ap[a.lo];
+    const T* Fn = a.buf + P.aphn[a.fin];
+    const T* Fa = a.buf + P.apha[a.fin];
+    const T* Fb = a.buf + P.aphb[a.fin];
+    T* Fn_o = a.buf + P.aphn[a.fin ^ 1];
+    T* Fa_o = a.buf + P.apha[a.fin ^ 1];
+    T* Fb_o = a.buf + P.aphb[a.fin ^ 1];
+    const T* zeta = a.buf + P.zeta;
+    const T* hp = zgrad ? a.hist_p + (hofs + 1) * a.hlen + P.hoff : nullptr;    // p(t)
+    const T* hpp = zgrad ? a.hist_p + hofs * a.hlen + P.hoff : nullptr;         // p(t-1)
+    const T* hfn = zgrad ? a.hist_phn + hofs * a.hlen + P.hoff : nullptr;       // phi_n(t)
+    // register windows along the normal: X(l-3 .. l+3), z Phi_n(l-2 .. l+2), p(t)(l-2 .. l+2)
+    T xw[7], zw[5], qw[5];
+#pragma unroll
+    for (int m = 0; m < 7; ++m) {
+      const int ll = m - 3;
+      xw[m] = (inside && ll >= 0 && ll < L) ? X[ll * lstride + col] : (T)0;
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const int ll = m - 2;
+      const bool ok = inside && ll >= 0 && ll < L;
+      zw[m] = ok ? zeta[ll] * Fn[ll * lstride + col] : (T)0;
+      qw[m] = (ok && zgrad) ? hp[ll * lstride + col] : (T)0;
+    }
+    T gacc[kMaxPmlLayers];
+#pragma unroll
+    for (int q = 0; q < kMaxPmlLayers; ++q) gacc[q] = 0;
+    const T d180 = (T)180 * a.dh * a.dh, d12 = (T)12 * a.dh;
+    for (int l = 0; l < L; ++l) {
+      const T* Xl = X + l * lstride;
+      const T* fal = Fa + l * lstride;
+      const T* fbl = Fb + l * lstride;
+      __syncthreads();  // previous layer done with the tiles
+      for (int i = threadIdx.x; i < (TA + 6) * (TB + 6); i += 256) {
+        const int r = i / (TB + 6), c = i - r * (TB + 6);
+        const int aa = a0 + r - 3, bb = b0 + c - 3;
+        Xs[r][c] = (aa >= 0 && aa < A && bb >= 0 && bb < B) ? Xl[(long long)aa * B + bb] : (T)0;
+      }
+      for (int i = threadIdx.x; i < (TA + 4) * TB; i += 256) {
+        const int r = i / TB, c = i - r * TB;
+        const int aa = a0 + r - 2, bb = b0 + c;
+        FA[r][c] = (aa >= 0 && aa < A && bb < B) ? fal[(long long)aa * B + bb] : (T)0;
+      }
+      for (int i = threadIdx.x; i < TA * (TB + 4); i += 256) {
+        const int r = i / (TB + 4), c = i - r * (TB + 4);
+        const int aa = a0 + r, bb = b0 + c - 2;
+        FB[r][c] = (aa < A && bb >= 0 && bb < B) ? fbl[(long long)aa * B + bb] : (T)0;
+      }
+      if (zgrad) {
+        const T* hpl = hp + l * lstride;
+        for (int i = threadIdx.x; i < (TA + 4) * (TB + 4); i += 256) {
+          const int r = i / (TB + 4), c = i - r * (TB + 4);
+          const int aa = a0 + r - 2, bb = b0 + c - 2;
+          Qs[r][c] = (aa >= 0 && aa < A && bb >= 0 && bb < B) ? hpl[(long long)aa * B + bb] : (T)0;
+        }
+      }
+      __syncthreads();
+      if (inside) {
+        T lx = 0;
+#pragma unroll
+        for (int m = 0; m < 7; ++m) lx += c7[m] * (xw[m] + Xs[ta + m][tb + 3] + Xs[ta + 3][tb + m]);
+        T dnx = 0, dax = 0, dbx = 0, dnz = 0, daf = 0, dbf = 0;
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+          dnx += c5[m] * xw[m + 1];
+          dax += c5[m] * Xs[ta + 1 + m][tb + 3];
+          dbx += c5[m] * Xs[ta + 3][tb + 1 + m];
+          dnz += c5[m] * zw[m];
+          daf += c5[m] * FA[ta + m][tb];
+          dbf += c5[m] * FB[ta][tb + m];
+        }
+        lx /= d180;
+        dnx /= d12; dax /= d12; dbx /= d12;
+        dnz /= d12; daf /= d12; dbf /= d12;
+        const long long I = l * lstride + col;
+        const T zn = zeta[l];
+        const T x0 = xw[3], y0 = Y[I];
+        const T fn0 = Fn[I], fa0 = FA[ta + 2][tb], fb0 = FB[ta][tb + 2];
+        O[I] = O[I] + (T)2 * x0 + dt2 * a.c0 * a.c0 * lx - dt * zn * x0 + (dt * zn - (T)1) * y0 + dt * dnz -
+               dt * zn * (daf + dbf);
+        Y[I] = 0;
+        Fn_o[I] = ((T)1 - dt * zn) * fn0 - dt2 * dnx;
+        Fa_o[I] = fa0 - dt2 * dax;
+        Fb_o[I] = fb0 - dt2 * dbx;
+        if (zgrad) {
+          T dnp = 0, dap = 0, dbp = 0;
+#pragma unroll
+          for (int m = 0; m < 5; ++m) {
+            dnp += c5[m] * qw[m];
+            dap += c5[m] * Qs[ta + m][tb + 2];
+            dbp += c5[m] * Qs[ta + 2][tb + m];
+          }
+          dnp /= d12; dap /= d12; dbp /= d12;
+          const T g = -dt * x0 * (qw[2] - hpp[I]) - dt * fn0 * (hfn[I] + dnp) + dt * (fa0 * dap + fb0 * dbp);
+#pragma unroll
+          for (int q = 0; q < kMaxPmlLayers; ++q)
+            if (q == l) gacc[q] += g;
+        }
+      }
+      // slide the windows one layer
+#pragma unroll
+      for (int m = 0; m < 6; ++m) xw[m] = xw[m + 1];
+      xw[6] = (inside && l + 4 < L) ? X[(l + 4) * lstride + col] : (T)0;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) { zw[m] = zw[m + 1]; qw[m] = qw[m + 1]; }
+      const bool ok3 = inside && l + 3 < L;
+      zw[4] = ok3 ? zeta[l + 3] * Fn[(l + 3) * lstride + col] : (T)0;
+      qw[4] = (ok3 && zgrad) ? hp[(l + 3) * lstride + col] : (T)0;
+    }
+    if (zgrad) {
+#pragma unroll
+      for (int q = 0; q < kMaxPmlLayers; ++q) {
+        const double s = warp_sum((double)gacc[q]);
+        if (lane == 0) red[warp][q] = s;
+      }
+      __syncthreads();
+      if (threadIdx.x < L) {
+        double s = 0;
+        for (int w8 = 0; w8 < 8; ++w8) s += red[w8][threadIdx.x];
+        a.gz[(long long)bi * kMaxPmlLayers + threadIdx.x] += s;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Source-series gradient, initial-pressure gradient, counters
+// ---------------------------------------------------------------------------
+
+// dJ/d series[slot][t] = s_f * (sum of the modal tiles' partials); one warp per source.
+// g is [steps][ld], columns = global source slots.
+template <typename T>
+__global__ void srcgrad_kernel(const T* __restrict__ buf, const DctDev* __restrict__ dct,
+                               const PointDev* __restrict__ srcs, int npts, int ld, double* __restrict__ g,
+                               const long long* tc, int tstep) {
+  const int lane = threadIdx.x & 31;
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= npts) return;
+  const PointDev q = srcs[r];
+  const DctDev& D = dct[q.part];
+  const int local = r - D.src0;
+  const int ntiles = D.nbx * D.nby * D.nbz;
+  T s = 0;
+  for (int i = lane; i < ntiles; i += 32) s += buf[D.srcpart + (long long)i * D.nsrc + local];
+  s = warp_sum(s);
+  const long long t = tc[0] - tstep;
+  if (lane == 0) g[t * ld + q.slot] = (double)s * D.sf;
+}
+
+// dJ/dm0 for modes that start at rest (M(-1) = M(-2) = m0):
+// (alpha - a) mu(0) - a mu(1), written unpadded [kz][ky][kx] at `out`.
+template <typename T, bool REF>
+__global__ void init_grad_kernel(T* buf, DctDev D, long long out) {
+  const long long N = (long long)D.w * D.h * D.d;
+  const T a = (T)D.damping;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % D.w);
+    const long long yz = i / D.w;
+    const long long pi = yz * D.wp + x;
+    const T ta = buf[D.tabA + pi];
+    const T c1 = REF ? a * ((T)2 * ta - (T)1) : a * ((T)1 - (T)2 * ta);
+    buf[out + i] = c1 * buf[D.AM[0] + pi] - a * buf[D.AM[1] + pi];
+  }
+}
+
+static __global__ void set_counters_kernel(long long* tc, long long t, long long t0) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) { tc[0] = t; tc[1] = t0; }
+}
+
+}  // namespace ard

@@ -60,6 +60,10 @@ struct DctDev {
   long long tmpX, tmpY, tmpZ;
   long long cw, ch, cd;    // cosine tables of extents w, h, d: C, Ci, C^T, Ci^T (n*n each)
   long long recpart;       // [ntiles][nrec]
+  long long srcpart;       // [ntiles][nsrc] (adjoint: source-gradient partials)
+  long long AM[2];         // adjoint of the modal levels
+  long long aX, aY, aZ;    // adjoint of the shell force
+  long long qX, qY, qZ;    // adjoint of the face pressure
   double sf;               // forward scale 1 / (2 sqrt(2N))
   double si;               // inverse scale 1 / sqrt(2N)
   double damping;
@@ -79,8 +83,12 @@ struct PmlDev {
   long long p[2];
   long long phn[2], pha[2], phb[2];
   long long force;        // [3][A][B]
+  long long ap[3];         // adjoint of p (three rotating levels)
+  long long aphn[2], apha[2], aphb[2];
+  long long aforce;        // adjoint of the strip force [3][A][B]
   long long zeta;         // [L] damping profile (scaled)
   long long n;            // L*A*B
+  long long hoff;         // offset of the slab inside each all-slab region (p, phi: same for all eight)
 };
 
 // Side of an interface: an air partition's face layers or a PML slab, both

@@ -121,6 +121,7 @@ extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_o
   ctx->use_graphs = opt ? (opt->use_graphs != 0) : true;
   ctx->device = opt ? opt->device : 0;
   ctx->arith = opt ? opt->arithmetic : ARD_ARITH_ACCURATE;
+  ctx->adjoint = opt ? (opt->adjoint != 0) : false;
   {
     const char* dbg = std::getenv("ARD_DEBUG_SYNC");
     ctx->debug_sync = dbg && dbg[0] == '1';
@@ -226,7 +227,7 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   ARD_CUDA(mark(kStagePml));
   if (!ctx->pml_blocks.empty()) {
     PmlArgs<T> pa{buf, ctx->d_pml, ctx->d_pml_blocks, (int)ctx->pml_blocks.size(), par,
-                  (T)ctx->dt, (T)ctx->dh, (T)ctx->c0};
+                  (T)ctx->dt, (T)ctx->dh, (T)ctx->c0, (const PmlHist<T>*)ctx->d_phist, ctx->d_t, tstep};
     pml_kernel<T><<<grid_for((long long)ctx->pml_blocks.size(), 1, ctx->num_sms * 8), 256, 0, sp>>>(pa);
     ARD_CUDA(cudaGetLastError());
   }

@@ -68,6 +68,16 @@ struct Ctx {
   int maxn = 0;
   long long pool_elems = 0;
   long long scratch = 0;          // dense-transform scratch (3 x largest air partition)
+  long long state_begin = 0, state_end = 0;  // checkpointed state block
+  long long adj_begin = 0, adj_end = 0;      // adjoint state block
+  long long pml_region[8][2] = {};           // all slabs' p0, p1, phn0, phn1, pha0, pha1, phb0, phb1
+  bool adjoint = false;
+  // adjoint face transforms (options.adjoint): fused 2D jobs and the two-pass
+  // GEMM form (q rows, q columns, R columns, R rows)
+  std::vector<Face2DJob> adj1_2d, adj2_2d;
+  JobList adjg[4];
+  long long q_begin = 0, q_end = 0;          // adjoint face pressure (zeroed every adjoint step)
+  bool adj_valid = false;                    // adjoint levels hold mu(0), mu(1) of the last ard_adjoint
 
   // device memory
   void* d_buf = nullptr;          // element pool (float or double)
@@ -86,6 +96,10 @@ struct Ctx {
   float* d_series = nullptr;
   double* d_hist = nullptr;
   long long* d_t = nullptr;
+  Face2DJob *d_adj1_2d = nullptr, *d_adj2_2d = nullptr;
+  XformJob* d_adjg[4] = {nullptr, nullptr, nullptr, nullptr};
+  long long* d_tb = nullptr;      // adjoint counters {current step, first step of the PML history}
+  void* d_phist = nullptr;        // PmlHist<T> read by the PML kernel (adjoint contexts only)
 
   cudaStream_t stream = nullptr, stream2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -104,6 +118,11 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
 int launch_steps_direct(Ctx* ctx, int n, cudaStream_t s);
 int ensure_graph(Ctx* ctx);
 int check_guards(Ctx* ctx);
+void build_adjoint_jobs(Ctx* ctx);
+void pml_profile_unit(const Ctx* ctx, int type, int L, std::vector<double>* out);
+template <typename T>
+int dense_transform_ex(Ctx* ctx, const DctDev& D, long long in, long long out, long long scratch, int which,
+                       bool transpose, double scale);
 size_t elem_size(const Ctx* ctx);
 
 }  // namespace ard

@@ -307,8 +307,10 @@ struct ModalArgs {
   const float* series;      // [n_sources][max_steps]
   long long max_steps;
   const long long* tcount;  // steps completed before the current launch sequence
-  int tstep;                // step offset inside the sequence
+  int tstep;                // step offset inside the sequence (adjoint: counted backwards)
   int par;
+  const T* resid;           // adjoint: recorder residuals [steps][n_rec_total]
+  int n_rec_total;
 };
 
 // Shared memory of the modal kernel, in elements of T: the ky-contraction
@@ -326,7 +328,16 @@ constexpr int kModalSmemElems =
 // rows: along kx by a shuffle butterfly (partial per kx tile), along ky
 // through shared memory (partial per ky tile), along kz in registers
 // (partial per kz tile).  REF selects the reference's arithmetic.
-template <typename T, bool REF>
+//
+// ADJ runs the transposed step of the adjoint, backwards in time, on the
+// adjoint modal levels mu: mu(t) = alpha mu(t+1) - a mu(t+2) + G(t), where
+// alpha and -a are the forward recurrence's coefficients of M(t-1) and M(t-2)
+// and G is the expansion of the adjoint face transforms with the REDFT01
+// weights plus the recorder residuals injected with the recorder basis.  The
+// contraction then runs on beta mu(t) (beta: the forward coefficient of the
+// force mode F) with the REDFT10 weights onto the face rows and onto the
+// source cells (source-series gradient partials).
+template <typename T, bool REF, bool ADJ = false>
 __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* ry_s = reinterpret_cast<T*>(smem_raw);
@@ -337,7 +348,7 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
   __shared__ int pts_y[2][kMaxPointsPerPart], pts_z[2][kMaxPointsPerPart];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   T* __restrict__ buf = a.buf;
-  const long long t = *a.tcount + a.tstep;
+  const long long t = ADJ ? (*a.tcount - a.tstep) : (*a.tcount + a.tstep);
 
   for (int tile_id = blockIdx.x; tile_id < a.ntiles; tile_id += gridDim.x) {
     const int4 tl = a.tiles[tile_id];
@@ -359,19 +370,35 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
     const T* Cwi = Cw + (long long)w * w;
     const T* Chi = Ch + (long long)h * h;
     const T* Cdi = Cd + (long long)d * d;
+    // injected points (sources; adjoint: recorders) and read-out points
+    // (recorders; adjoint: sources) with their bases
+    const int ninj = ADJ ? nrec : nsrc, nout = ADJ ? nsrc : nrec;
+    const PointDev* injp = ADJ ? a.recs + D.rec0 : a.srcs + D.src0;
+    const PointDev* outp = ADJ ? a.srcs + D.src0 : a.recs + D.rec0;
+    const T* Iw = ADJ ? Cwi : Cw;
+    const T* Ih = ADJ ? Chi : Ch;
+    const T* Id = ADJ ? Cdi : Cd;
+    const T* Ow = ADJ ? Cw : Cwi;
+    const T* Oh = ADJ ? Ch : Chi;
+    const T* Od = ADJ ? Cd : Cdi;
 
     __syncthreads();  // the previous tile is done with shared memory
-    for (int i = tid; i < nsrc * KXT; i += kModalThreads) {
+    for (int i = tid; i < ninj * KXT; i += kModalThreads) {
       const int s = i / KXT, kl = i - s * KXT, kx = tl.y * KXT + kl;
-      const PointDev q = a.srcs[D.src0 + s];
-      const float v = (t < a.max_steps) ? a.series[(long long)q.slot * a.max_steps + t] : 0.0f;
-      cws[s * 128 + kl] = kx < w ? (T)D.sf * (T)v * Cw[(long long)kx * w + q.x] : (T)0;
+      const PointDev q = injp[s];
+      if constexpr (ADJ) {
+        const T v = a.resid[t * a.n_rec_total + q.slot];
+        cws[s * 128 + kl] = kx < w ? (T)D.si * v * Iw[(long long)kx * w + q.x] : (T)0;
+      } else {
+        const float v = (t < a.max_steps) ? a.series[(long long)q.slot * a.max_steps + t] : 0.0f;
+        cws[s * 128 + kl] = kx < w ? (T)D.sf * (T)v * Iw[(long long)kx * w + q.x] : (T)0;
+      }
       if (kl == 0) { pts_y[0][s] = q.y; pts_z[0][s] = q.z; }
     }
-    for (int i = tid; i < nrec * KXT; i += kModalThreads) {
+    for (int i = tid; i < nout * KXT; i += kModalThreads) {
       const int r = i / KXT, kl = i - r * KXT, kx = tl.y * KXT + kl;
-      const PointDev q = a.recs[D.rec0 + r];
-      cwr[r * 128 + kl] = kx < w ? Cwi[(long long)kx * w + q.x] : (T)0;
+      const PointDev q = outp[r];
+      cwr[r * 128 + kl] = kx < w ? Ow[(long long)kx * w + q.x] : (T)0;
       if (kl == 0) { pts_y[1][r] = q.y; pts_z[1][r] = q.z; }
     }
     __syncthreads();
@@ -391,6 +418,9 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
 #pragma unroll
     for (int n = 0; n < 3; ++n) cy[n] = Ch[(long long)kyc * h + n];
     const T wy = (ky == 0) ? (T)0.5 : (T)1;
+    // the REDFT01 halving of the k = 0 rows sits in the contraction (forward)
+    // or in the expansion (adjoint)
+    const T wxc = ADJ ? (T)1 : wx0, wyc = ADJ ? (T)1 : wy;
     const int pyr = ky & 1;
     const long long planeX = (long long)d * h, planeY = (long long)d * wp, planeZ = (long long)h * wp;
     const T* PX = buf + D.PX;
@@ -412,8 +442,8 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
     T racc[kMaxPointsPerPart];
 #pragma unroll
     for (int r = 0; r < kMaxPointsPerPart; ++r) racc[r] = 0;
-    const T* Mcur = buf + D.M[a.par ^ 1];   // M(t-1)
-    T* Mout = buf + D.M[a.par];             // holds M(t-2); receives M(t)
+    const T* Mcur = buf + (ADJ ? D.AM[a.par ^ 1] : D.M[a.par ^ 1]);   // M(t-1) (adjoint: mu(t+1))
+    T* Mout = buf + (ADJ ? D.AM[a.par] : D.M[a.par]);                 // M(t-2) -> M(t) (adjoint: mu(t+2) -> mu(t))
     const T* tabA = buf + D.tabA;
     const T* tabB = buf + D.tabB;
     const T damping = (T)D.damping;
@@ -444,6 +474,7 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
 #pragma unroll
       for (int n = 0; n < 3; ++n) cz[n] = Cd[(long long)kz * d + n];
       const T wz = (kz == 0) ? (T)0.5 : (T)1;
+      const T wzc = ADJ ? (T)1 : wz;
       T px[2][3];
 #pragma unroll
       for (int pm = 0; pm < 2; ++pm)
@@ -465,33 +496,63 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
       T F[4];
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        T f = 0;
+        if constexpr (ADJ) {
+          T fx = 0, fy = 0, fz = 0;
 #pragma unroll
-        for (int n = 0; n < 3; ++n) f += cx[e][n] * px[e & 1][n];
+          for (int n = 0; n < 3; ++n) {
+            fx += cx[e][n] * px[e & 1][n];
+            fy += cy[n] * py[n][e];
+            fz += cz[n] * pz[PZ][n][e];
+          }
+          F[e] = (e == 0 ? wx0 : (T)1) * fx + wy * fy + wz * fz;
+        } else {
+          T f = 0;
 #pragma unroll
-        for (int n = 0; n < 3; ++n) f += cy[n] * py[n][e];
+          for (int n = 0; n < 3; ++n) f += cx[e][n] * px[e & 1][n];
 #pragma unroll
-        for (int n = 0; n < 3; ++n) f += cz[n] * pz[PZ][n][e];
-        F[e] = f;
+          for (int n = 0; n < 3; ++n) f += cy[n] * py[n][e];
+#pragma unroll
+          for (int n = 0; n < 3; ++n) f += cz[n] * pz[PZ][n][e];
+          F[e] = f;
+        }
       }
-      for (int s = 0; s < nsrc; ++s) {
-        const T coef = Ch[(long long)kyc * h + pts_y[0][s]] * Cd[(long long)kz * d + pts_z[0][s]];
+      for (int s = 0; s < ninj; ++s) {
+        const T coef = Ih[(long long)kyc * h + pts_y[0][s]] * Id[(long long)kz * d + pts_z[0][s]];
         T c[4];
         load4(cws + s * 128 + kl0, c);
 #pragma unroll
         for (int e = 0; e < 4; ++e) F[e] += c[e] * coef;
       }
       T Mn[4];
+      if constexpr (ADJ) {
+        T beta[4];
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        T v;
-        if (REF)  // dct_partition.cpp:68: a (2 M cwt - M_prev + (2 F / w2) (1 - cwt))
-          v = damping * ((T)2 * m[e] * ta[e] - mp[e] + ((T)2 * F[e] / tb[e]) * ((T)1 - ta[e]));
-        else      // the same recurrence with ta = 1 - cwt, tb = 2 (1 - cwt) / w2
-          v = damping * (((T)2 * m[e] - mp[e]) - (T)2 * ta[e] * m[e] + tb[e] * F[e]);
-        Mn[e] = act[e] ? v : (T)0;
+        for (int e = 0; e < 4; ++e) {
+          T v;
+          if (REF) {
+            v = damping * ((T)2 * m[e] * ta[e] - mp[e]) + F[e];
+            beta[e] = damping * ((T)2 / tb[e]) * ((T)1 - ta[e]);
+          } else {
+            v = damping * (((T)2 * m[e] - mp[e]) - (T)2 * ta[e] * m[e]) + F[e];
+            beta[e] = damping * tb[e];
+          }
+          Mn[e] = act[e] ? v : (T)0;
+        }
+        if (lanok) store4(Mout + row, Mn);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) Mn[e] *= beta[e];   // contracted: the adjoint of the force mode
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          T v;
+          if (REF)  // dct_partition.cpp:68: a (2 M cwt - M_prev + (2 F / w2) (1 - cwt))
+            v = damping * ((T)2 * m[e] * ta[e] - mp[e] + ((T)2 * F[e] / tb[e]) * ((T)1 - ta[e]));
+          else      // the same recurrence with ta = 1 - cwt, tb = 2 (1 - cwt) / w2
+            v = damping * (((T)2 * m[e] - mp[e]) - (T)2 * ta[e] * m[e] + tb[e] * F[e]);
+          Mn[e] = act[e] ? v : (T)0;
+        }
+        if (lanok) store4(Mout + row, Mn);
       }
-      if (lanok) store4(Mout + row, Mn);
       // contraction along kz (registers) and ky (shared memory, reduced below)
       T* slot = ry_s + PZ * kModalRySlot;
 #pragma unroll
@@ -499,8 +560,8 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
         T ry[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-          rz[PZ][n][e] += wz * cz[n] * Mn[e];
-          ry[e] = wy * cy[n] * Mn[e];
+          rz[PZ][n][e] += wzc * cz[n] * Mn[e];
+          ry[e] = wyc * cy[n] * Mn[e];
         }
         store4(slot + n * 1024 + rs * KXT + kl0, ry);
       }
@@ -508,7 +569,7 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
       T v[6];
 #pragma unroll
       for (int n = 0; n < 3; ++n) {
-        v[n] = wx0 * cx[0][n] * Mn[0] + cx[2][n] * Mn[2];
+        v[n] = wxc * cx[0][n] * Mn[0] + cx[2][n] * Mn[2];
         v[3 + n] = cx[1][n] * Mn[1] + cx[3][n] * Mn[3];
       }
       for (int o = G >> 1; o > 0; o >>= 1)
@@ -521,8 +582,8 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
           if (li == q) val = v[q];
         buf[D.RX + ((long long)tl.y * 6 + li) * planeX + (long long)kz * h + ky] = val;
       }
-      for (int r = 0; r < nrec; ++r) {
-        const T coef = Chi[(long long)kyc * h + pts_y[1][r]] * Cdi[(long long)kz * d + pts_z[1][r]];
+      for (int r = 0; r < nout; ++r) {
+        const T coef = Oh[(long long)kyc * h + pts_y[1][r]] * Od[(long long)kz * d + pts_z[1][r]];
         T c[4];
         load4(cwr + r * 128 + kl0, c);
         racc[r] += coef * (c[0] * Mn[0] + c[1] * Mn[1] + c[2] * Mn[2] + c[3] * Mn[3]);
@@ -566,20 +627,20 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
         for (int n = 0; n < 3; ++n)
           store4(buf + D.RZ + ((long long)tl.w * 6 + pm * 3 + n) * planeZ + (long long)ky * wp + kx0, rz[pm][n]);
     }
-    if (nrec > 0) {
+    if (nout > 0) {
 #pragma unroll
       for (int r = 0; r < kMaxPointsPerPart; ++r) {
-        if (r < nrec) {
+        if (r < nout) {
           const T s = warp_sum(racc[r]);
           if (lane == 0) red[warp * kMaxPointsPerPart + r] = s;
         }
       }
       __syncthreads();
-      if (tid < nrec) {
+      if (tid < nout) {
         T s = 0;
         for (int k = 0; k < kModalThreads / 32; ++k) s += red[k * kMaxPointsPerPart + tid];
         const int local = (tl.y * D.nby + tl.z) * D.nbz + tl.w;
-        buf[D.recpart + (long long)local * nrec + tid] = s;
+        buf[(ADJ ? D.srcpart : D.recpart) + (long long)local * nout + tid] = s;
       }
     }
   }
@@ -608,6 +669,18 @@ __global__ void recorder_kernel(const T* __restrict__ buf, const DctDev* __restr
 // PML
 // ---------------------------------------------------------------------------
 
+// Forward PML history kept for the adjoint's damping gradient: for steps
+// t0 <= t < t1 the PML kernel also writes p(t) to p[(t - t0 + 1) hlen + ...]
+// and phi_n(t) to phn[(t - t0) hlen + ...] (all-slab region layout, slab at
+// PmlDev::hoff).  p == null: nothing is kept.
+template <typename T>
+struct PmlHist {
+  T* p;
+  T* phn;
+  long long hlen;
+  long long t0, t1;
+};
+
 template <typename T>
 struct PmlArgs {
   T* buf;
@@ -616,6 +689,9 @@ struct PmlArgs {
   int nblocks;
   int par;
   T dt, dh, c0;
+  const PmlHist<T>* hist;   // null without the adjoint
+  const long long* tcount;
+  int tstep;
 };
 
 // Grote-Sim PML (pml_partition.cpp:113-200) in slab coordinates: layer l
@@ -634,6 +710,16 @@ __global__ void __launch_bounds__(256) pml_kernel(PmlArgs<T> a) {
   const T c7[7] = {2, -27, 270, -490, 270, -27, 2};
   const T c5[5] = {1, -8, 0, 8, -1};
   const int tb = threadIdx.x & 31, ta = threadIdx.x >> 5;
+  T* hp = nullptr;
+  T* hfn = nullptr;
+  if (a.hist) {
+    const PmlHist<T> h = *a.hist;
+    const long long t = *a.tcount + a.tstep;
+    if (h.p && t >= h.t0 && t < h.t1) {
+      hp = h.p + (t - h.t0 + 1) * h.hlen;
+      hfn = h.phn + (t - h.t0) * h.hlen;
+    }
+  }
   for (int bi = blockIdx.x; bi < a.nblocks; bi += gridDim.x) {
     const int4 blk = a.blocks[bi];
     const PmlDev& P = a.pml[blk.x];
@@ -715,9 +801,15 @@ __global__ void __launch_bounds__(256) pml_kernel(PmlArgs<T> a) {
         const T f = (sl >= 0 && sl < 3) ? force[sl * lstride + col] : (T)0;
         const T t3 = a.c0 * a.c0 * (ln + la + lb);
         const T t4 = -zn * (pcur - pold) / a.dt;
-        pn[I] = (T)2 * pcur - pold + a.dt * a.dt * (t3 + t4 + (gn + ga + gb) + f);
+        const T pnew = (T)2 * pcur - pold + a.dt * a.dt * (t3 + t4 + (gn + ga + gb) + f);
+        pn[I] = pnew;
         const T fnc = fw[2];
-        fn_o[I] = fnc - a.dt * zn * fnc + a.dt * (-zn) * un;
+        const T fnew = fnc - a.dt * zn * fnc + a.dt * (-zn) * un;
+        fn_o[I] = fnew;
+        if (hp) {
+          hp[P.hoff + I] = pnew;
+          hfn[P.hoff + I] = fnew;
+        }
         fa_o[I] = FA[ta + 2][tb] + a.dt * zn * ua;
         fb_o[I] = FB[ta][tb + 2] + a.dt * zn * ub;
       }

@@ -79,6 +79,12 @@ void pml_profile(const Ctx* ctx, int type, int L, double scale, std::vector<doub
 
 }  // namespace
 
+// Damping profile of a slab for face scale 1 (zeta is linear in the scale).
+void pml_profile_unit(const Ctx* ctx, int type, int L, std::vector<double>* out) {
+  if (ctx->prec == ARD_PREC_F64) pml_profile<double>(ctx, type, L, 1.0, out);
+  else pml_profile<float>(ctx, type, L, 1.0, out);
+}
+
 // Reference-arithmetic modal tables, computed on the host exactly as
 // DctPartition's constructor does (dct_partition.cpp:24-36): 1-based mode
 // numbers, w and cos(w dt) in the working precision with the C library's
@@ -125,28 +131,91 @@ int upload_pml_zeta(Ctx* ctx) {
 
 int zero_state(Ctx* ctx) {
   const size_t es = elem_size(ctx);
-  for (const DctDev& D : ctx->dct) {
-    const long long Np = (long long)D.wp * D.h * D.d;
-    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.M[0] * es, 0, Np * es, ctx->stream));
-    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.M[1] * es, 0, Np * es, ctx->stream));
-    // fX..fZ and pX..pZ are contiguous runs
-    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.fX * es, 0, (D.fZ - D.fX + 6LL * D.h * D.wp) * es, ctx->stream));
-    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + D.pX * es, 0, (D.pZ - D.pX + 6LL * D.h * D.wp) * es, ctx->stream));
-  }
-  for (const PmlDev& P : ctx->pml) {
-    for (int k = 0; k < 2; ++k) {
-      ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + P.p[k] * es, 0, P.n * es, ctx->stream));
-      ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + P.phn[k] * es, 0, P.n * es, ctx->stream));
-      ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + P.pha[k] * es, 0, P.n * es, ctx->stream));
-      ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + P.phb[k] * es, 0, P.n * es, ctx->stream));
-    }
-    ARD_CUDA(cudaMemsetAsync((char*)ctx->d_buf + P.force * es, 0, 3LL * P.A * P.B * es, ctx->stream));
-  }
+  char* base = (char*)ctx->d_buf;
+  ARD_CUDA(cudaMemsetAsync(base + ctx->state_begin * es, 0, (ctx->state_end - ctx->state_begin) * es, ctx->stream));
+  if (ctx->adjoint)
+    ARD_CUDA(cudaMemsetAsync(base + ctx->adj_begin * es, 0, (ctx->adj_end - ctx->adj_begin) * es, ctx->stream));
   ARD_CUDA(cudaMemsetAsync(ctx->d_t, 0, sizeof(long long), ctx->stream));
   if (ctx->n_rec_total > 0)
     ARD_CUDA(cudaMemsetAsync(ctx->d_hist, 0, sizeof(double) * ctx->max_steps * ctx->n_rec_total, ctx->stream));
   ctx->t_host = 0;
   return ARD_OK;
+}
+
+// Face transforms of the adjoint step, the transposes of the forward ones:
+//   adjoint of the inverse transform: Q[pm][n] = s_i Ci_V (q_n +/- q_{5-n}) Ci_U^T
+//     (the adjoint face pressure q -> the P arrays read by the adjoint modal step)
+//   adjoint of the forward transform: a_L = s_f C_V^T (sum of R partials, combined
+//     as for the inverse) C_U (-> the adjoint shell force)
+// as fused 2D jobs and as two-pass GEMM jobs.
+void build_adjoint_jobs(Ctx* ctx) {
+  auto add_job = [](JobList& list, XformJob j) {
+    const int Md = j.rows ? j.batch : j.n, Nd = j.rows ? j.n : j.batch;
+    j.tn = (Nd + 63) / 64;
+    j.ntiles = ((Md + 63) / 64) * j.tn;
+    list.add(j, j.ntiles);
+  };
+  for (const DctDev& D : ctx->dct) {
+    struct Ax { long long q, a, P, R, tmp; int U, V, ld; long long cU, cV; int nb; };
+    const Ax axes[3] = {{D.qX, D.aX, D.PX, D.RX, D.tmpX, D.h, D.d, D.h, D.ch, D.cd, D.nbx},
+                        {D.qY, D.aY, D.PY, D.RY, D.tmpY, D.w, D.d, D.wp, D.cw, D.cd, D.nby},
+                        {D.qZ, D.aZ, D.PZ, D.RZ, D.tmpZ, D.w, D.h, D.wp, D.cw, D.ch, D.nbz}};
+    for (const Ax& a : axes) {
+      const long long LS = (long long)a.V * a.ld;
+      const long long UU = (long long)a.U * a.U, VV = (long long)a.V * a.V;
+      for (int u0 = 0; u0 < a.U; u0 += 32) {
+        const int ub = std::min(32, a.U - u0);
+        for (int pm = 0; pm < 2; ++pm)
+          for (int n = 0; n < 3; ++n) {
+            Face2DJob j{};
+            j.in0 = a.q + n * LS; j.in1 = a.q + (5 - n) * LS; j.sgn = pm ? -1 : 1;
+            j.nparts = 1; j.part_stride = 0;
+            j.out = a.P + (pm * 3 + n) * LS;
+            j.tabA = a.cV + VV; j.tabB = a.cU + 3 * UU;   // Ci_V, Ci_U^T
+            j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.si;
+            ctx->adj1_2d.push_back(j);
+          }
+        for (int L = 0; L < 6; ++L) {
+          const int n = L < 3 ? L : 5 - L;
+          Face2DJob j{};
+          j.in0 = a.R + n * LS; j.in1 = a.R + (3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
+          j.nparts = a.nb; j.part_stride = 6 * LS;
+          j.out = a.a + L * LS;
+          j.tabA = a.cV + 2 * VV; j.tabB = a.cU;          // C_V^T, C_U
+          j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.sf;
+          ctx->adj2_2d.push_back(j);
+        }
+      }
+      // two-pass GEMM form (partitions whose layers do not fit in shared memory)
+      for (int pm = 0; pm < 2; ++pm)
+        for (int n = 0; n < 3; ++n) {
+          XformJob j{};   // rows along U with Ci_U: A(o, j) = Ci_U[o][j]
+          j.in0 = a.q + n * LS; j.in1 = a.q + (5 - n) * LS; j.sgn = pm ? -1 : 1;
+          j.out = a.tmp + (pm * 3 + n) * LS; j.ctab = a.cU + UU; j.n = a.U; j.batch = a.V; j.ld = a.ld;
+          j.nparts = 1; j.part_stride = 0; j.inverse = 0; j.rows = 1; j.scale = 1.0;
+          add_job(ctx->adjg[0], j);
+          XformJob k{};   // columns along V with Ci_V
+          k.in0 = a.tmp + (pm * 3 + n) * LS; k.in1 = -1; k.sgn = 1;
+          k.out = a.P + (pm * 3 + n) * LS; k.ctab = a.cV + VV; k.n = a.V; k.batch = a.U; k.ld = a.ld;
+          k.nparts = 1; k.part_stride = 0; k.inverse = 0; k.rows = 0; k.scale = D.si;
+          add_job(ctx->adjg[1], k);
+        }
+      for (int L = 0; L < 6; ++L) {
+        const int n = L < 3 ? L : 5 - L;
+        XformJob j{};     // columns along V with C_V^T: A(o, r) = C_V[r][o]
+        j.in0 = a.R + (0 * 3 + n) * LS; j.in1 = a.R + (1 * 3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
+        j.nparts = a.nb; j.part_stride = 6 * LS;
+        j.out = a.tmp + L * LS; j.ctab = a.cV; j.n = a.V; j.batch = a.U; j.ld = a.ld;
+        j.inverse = 1; j.rows = 0; j.scale = 1.0;
+        add_job(ctx->adjg[2], j);
+        XformJob k{};     // rows along U with C_U: A(o, j) = C_U[j][o]
+        k.in0 = a.tmp + L * LS; k.in1 = -1; k.sgn = 1; k.nparts = 1; k.part_stride = 0;
+        k.out = a.a + L * LS; k.ctab = a.cU; k.n = a.U; k.batch = a.V; k.ld = a.ld;
+        k.inverse = 1; k.rows = 1; k.scale = D.sf;
+        add_job(ctx->adjg[3], k);
+      }
+    }
+  }
 }
 
 int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
@@ -192,12 +261,10 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         const long long N = (long long)D.w * D.h * D.d;
         const long long Np = (long long)D.wp * D.h * D.d;
         ctx->n_air_cells += N;
-        D.M[0] = pool.take(Np); D.M[1] = pool.take(Np);
-        D.tabA = pool.take(Np); D.tabB = pool.take(Np);
+        (void)Np;
         D.damping = sc.modal_damping;
         D.sf = 1.0 / (2.0 * std::sqrt(2.0 * (double)N));
         D.si = 1.0 / std::sqrt(2.0 * (double)N);
-        D.cw = cos_table(D.w); D.ch = cos_table(D.h); D.cd = cos_table(D.d);
         rec.engine_idx[i] = (int)ctx->dct.size();
         ctx->dct.push_back(D);
       } else {
@@ -298,14 +365,64 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     for (int bx = 0; bx < D.nbx; ++bx)
       for (int by = 0; by < D.nby; ++by)
         for (int bz = 0; bz < D.nbz; ++bz) ctx->tiles.push_back(make_int4((int)k, bx, by, bz));
-    // face arrays (Y and Z layers use the padded row pitch wp)
+  }
+
+  // ---- state block: everything a checkpoint holds, contiguous ----
+  // (modal levels, shell forces, PML fields and strips; the adjoint's carried
+  // state follows in a block of its own)
+  auto faces = [](const DctDev& D) { return 6LL * D.d * D.h + 6LL * D.d * D.wp + 6LL * D.h * D.wp; };
+  auto set_faces = [](DctDev& D, long long base, long long* fx, long long* fy, long long* fz) {
+    *fx = base; *fy = base + 6LL * D.d * D.h; *fz = *fy + 6LL * D.d * D.wp;
+  };
+  ctx->state_begin = pool.off;
+  for (DctDev& D : ctx->dct) D.M[0] = pool.take((long long)D.wp * D.h * D.d);
+  for (DctDev& D : ctx->dct) D.M[1] = pool.take((long long)D.wp * D.h * D.d);
+  for (DctDev& D : ctx->dct) set_faces(D, pool.take(faces(D)), &D.fX, &D.fY, &D.fZ);
+  for (int q = 0; q < 8; ++q) {
+    ctx->pml_region[q][0] = pool.off;
+    for (PmlDev& P : ctx->pml) {
+      long long* slot[8] = {&P.p[0], &P.p[1], &P.phn[0], &P.phn[1], &P.pha[0], &P.pha[1], &P.phb[0], &P.phb[1]};
+      *slot[q] = pool.take(P.n);
+    }
+    ctx->pml_region[q][1] = pool.off;
+  }
+  for (PmlDev& P : ctx->pml) P.force = pool.take(3LL * P.A * P.B);
+  ctx->state_end = pool.off;
+  // a slab sits at the same offset inside each of the eight regions
+  for (PmlDev& P : ctx->pml) {
+    P.hoff = P.p[0] - ctx->pml_region[0][0];
+    const long long* slot[8] = {&P.p[0], &P.p[1], &P.phn[0], &P.phn[1], &P.pha[0], &P.pha[1], &P.phb[0], &P.phb[1]};
+    for (int q = 0; q < 8; ++q)
+      if (*slot[q] - ctx->pml_region[q][0] != P.hoff) { ctx->err = "internal: PML regions out of step"; return ARD_ERR_STATE; }
+  }
+  if (ctx->adjoint) {
+    ctx->adj_begin = pool.off;
+    for (DctDev& D : ctx->dct) D.AM[0] = pool.take((long long)D.wp * D.h * D.d);
+    for (DctDev& D : ctx->dct) D.AM[1] = pool.take((long long)D.wp * D.h * D.d);
+    for (DctDev& D : ctx->dct) set_faces(D, pool.take(faces(D)), &D.aX, &D.aY, &D.aZ);   // adjoint of the shell force
+    ctx->q_begin = pool.off;
+    for (DctDev& D : ctx->dct) set_faces(D, pool.take(faces(D)), &D.qX, &D.qY, &D.qZ);   // adjoint of the face pressure
+    ctx->q_end = pool.off;
+    for (PmlDev& P : ctx->pml) {
+      for (int k = 0; k < 3; ++k) P.ap[k] = pool.take(P.n);
+      for (int k = 0; k < 2; ++k) { P.aphn[k] = pool.take(P.n); P.apha[k] = pool.take(P.n); P.aphb[k] = pool.take(P.n); }
+      P.aforce = pool.take(3LL * P.A * P.B);
+    }
+    ctx->adj_end = pool.off;
+  }
+
+  // ---- constants and per-step scratch ----
+  for (DctDev& D : ctx->dct) {
+    const long long Np = (long long)D.wp * D.h * D.d;
+    D.tabA = pool.take(Np); D.tabB = pool.take(Np);
+    D.cw = cos_table(D.w); D.ch = cos_table(D.h); D.cd = cos_table(D.d);
     const long long FX = 6LL * D.d * D.h, FY = 6LL * D.d * D.wp, FZ = 6LL * D.h * D.wp;
-    D.fX = pool.off; D.fY = D.fX + FX; D.fZ = D.fY + FY; pool.take(FX + FY + FZ);
-    D.pX = pool.off; D.pY = D.pX + FX; D.pZ = D.pY + FY; pool.take(FX + FY + FZ);
+    set_faces(D, pool.take(faces(D)), &D.pX, &D.pY, &D.pZ);
     D.PX = pool.take(FX); D.PY = pool.take(FY); D.PZ = pool.take(FZ);
     D.RX = pool.take(FX * D.nbx); D.RY = pool.take(FY * D.nby); D.RZ = pool.take(FZ * D.nbz);
     D.tmpX = pool.take(FX); D.tmpY = pool.take(FY); D.tmpZ = pool.take(FZ);
     D.recpart = pool.take(std::max(1, D.nrec) * (long long)D.nbx * D.nby * D.nbz);
+    D.srcpart = pool.take(std::max(1, D.nsrc) * (long long)D.nbx * D.nby * D.nbz);
   }
 
   // ---- dense-transform scratch (initial pressure, field readout): 3 x the largest air partition ----
@@ -322,10 +439,6 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
       ctx->err = "PML thicker than " + std::to_string(kMaxPmlLayers) + " layers";
       return ARD_ERR_INVALID;
     }
-    for (int q = 0; q < 2; ++q) {
-      P.p[q] = pool.take(P.n); P.phn[q] = pool.take(P.n); P.pha[q] = pool.take(P.n); P.phb[q] = pool.take(P.n);
-    }
-    P.force = pool.take(3LL * P.A * P.B);
     P.zeta = pool.take(P.L);
     ctx->n_pml_cells += P.n;
     for (int a0 = 0; a0 < P.A; a0 += 8)
@@ -558,6 +671,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     ctx->f2d_bytes = (size_t)(xs + bs + ts) * es0;
     ctx->fused_faces = !ctx->dct.empty() && ctx->f2d_bytes <= (size_t)std::min(ctx->smem_optin, 200 * 1024);
   }
+  if (ctx->adjoint) build_adjoint_jobs(ctx);
 
   // ---- device allocation ----
   const size_t es = elem_size(ctx);
@@ -598,6 +712,16 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   if ((rc = up(&ctx->d_inv2, ctx->inv2.jobs))) return rc;
   if ((rc = up(&ctx->d_fwd2d, ctx->fwd2d))) return rc;
   if ((rc = up(&ctx->d_inv2d, ctx->inv2d))) return rc;
+  if (ctx->adjoint) {
+    if ((rc = up(&ctx->d_adj1_2d, ctx->adj1_2d))) return rc;
+    if ((rc = up(&ctx->d_adj2_2d, ctx->adj2_2d))) return rc;
+    for (int k = 0; k < 4; ++k)
+      if ((rc = up(&ctx->d_adjg[k], ctx->adjg[k].jobs))) return rc;
+    ARD_CUDA(cudaMalloc(&ctx->d_tb, 2 * sizeof(long long)));
+    ARD_CUDA(cudaMemset(ctx->d_tb, 0, 2 * sizeof(long long)));
+    ARD_CUDA(cudaMalloc(&ctx->d_phist, sizeof(PmlHist<double>)));
+    ARD_CUDA(cudaMemset(ctx->d_phist, 0, sizeof(PmlHist<double>)));
+  }
   ARD_CUDA(cudaMalloc(&ctx->d_series, sizeof(float) * std::max(1LL, (long long)ctx->n_src_total * ctx->max_steps)));
   ARD_CUDA(cudaMemset(ctx->d_series, 0, sizeof(float) * (long long)ctx->n_src_total * ctx->max_steps));
   ARD_CUDA(cudaMalloc(&ctx->d_hist, sizeof(double) * std::max(1LL, (long long)ctx->n_rec_total * ctx->max_steps)));
@@ -644,7 +768,8 @@ void free_ctx_device(Ctx* ctx) {
   void* ptrs[] = {ctx->d_buf_base, ctx->d_mask, ctx->d_dct, ctx->d_pml, ctx->d_pml_blocks, ctx->d_ifs, ctx->d_srcpts,
                   ctx->d_recpts, ctx->d_tiles, ctx->d_fwd1, ctx->d_fwd2, ctx->d_inv1, ctx->d_inv2, ctx->d_fwd2d,
                   ctx->d_inv2d, ctx->d_series,
-                  ctx->d_hist, ctx->d_t};
+                  ctx->d_hist, ctx->d_t, ctx->d_adj1_2d, ctx->d_adj2_2d, ctx->d_adjg[0], ctx->d_adjg[1],
+                  ctx->d_adjg[2], ctx->d_adjg[3], ctx->d_tb, ctx->d_phist};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
@@ -663,11 +788,20 @@ void free_ctx_device(Ctx* ctx) {
 template <typename T>
 int dense_transform(Ctx* ctx, const DctDev& D, long long in, long long out, long long scratch, bool inverse,
                     double scale) {
+  return dense_transform_ex<T>(ctx, D, in, out, scratch, inverse ? 1 : 0, inverse, scale);
+}
+
+// General form: `table` 0 applies C, 1 applies Ci, each transposed when
+// `transpose` (C^T on every axis is the transpose of the forward transform).
+template <typename T>
+int dense_transform_ex(Ctx* ctx, const DctDev& D, long long in, long long out, long long scratch, int which,
+                       bool transpose, double scale) {
   T* buf = reinterpret_cast<T*>(ctx->d_buf);
   const long long plane = (long long)D.h * D.w;
+  const bool inverse = transpose;
   auto table = [&](int n) {
     for (auto& kv : ctx->cos_tables)
-      if (kv.first == n) return kv.second + (inverse ? (long long)n * n : 0);
+      if (kv.first == n) return kv.second + (which ? (long long)n * n : 0);
     return -1LL;
   };
   auto make = [&](long long i0, long long o0, int n, int batch, int ld, int rows, double sc) {
@@ -714,6 +848,8 @@ int dense_transform(Ctx* ctx, const DctDev& D, long long in, long long out, long
 
 template int dense_transform<float>(Ctx*, const DctDev&, long long, long long, long long, bool, double);
 template int dense_transform<double>(Ctx*, const DctDev&, long long, long long, long long, bool, double);
+template int dense_transform_ex<float>(Ctx*, const DctDev&, long long, long long, long long, int, bool, double);
+template int dense_transform_ex<double>(Ctx*, const DctDev&, long long, long long, long long, int, bool, double);
 
 }  // namespace ard
 

@@ -170,6 +170,7 @@ typedef struct ard_options {
   int32_t device;        /* CUDA device ordinal */
   int32_t autotune;      /* pick kernel tile shapes per extent by timing (default 0) */
   int32_t arithmetic;    /* ARD_ARITH_ACCURATE (default) or ARD_ARITH_REFERENCE */
+  int32_t adjoint;       /* nonzero: allocate the adjoint state (needed by ard_adjoint) */
 } ard_options;
 
 /* Modal-update arithmetic of the air partitions.
@@ -253,18 +254,25 @@ int ard_read_field_noalloc(ard_ctx* ctx, int32_t scene, int32_t partition, float
 
 /* ---- adjoint (gradients of a recorder misfit) ---- */
 
-/* Gradients of J = 0.5 * sum_{t<T} sum_r w_r (rec[t][r] - target[t][r])^2
- * over the first T steps of every scene, computed by the hand-written adjoint
- * kernels with checkpoints of the two modal time levels (and PML state)
- * every `checkpoint_every` steps and recomputation in between.  The forward
- * run is done inside this call from the current initial state (reset first).
- * target: T * n_recorders floats per scene, concatenated over scenes.
- * Outputs (any may be NULL), concatenated over scenes:
- *   grad_source  T * n_sources floats per scene    dJ/d(source series)
- *   grad_scale   6 floats per scene                dJ/d(PML face scale)
+/* Gradients of the recorder misfit
+ *   J = 0.5 * sum_{t<T} sum_r (rec[t][r] - target[t][r])^2      (per scene)
+ * computed by the hand-written adjoint step run backwards in time.  The
+ * call runs the forward itself from the current state, which must be step
+ * 0 (ard_reset, then ard_set_initial_pressure as wanted); on return the
+ * forward state and the recorder samples are those after step T, as if
+ * ard_step(T) had been called.  The context needs options.adjoint.
+ * target: T * n_recorders floats per scene ([t][recorder]), concatenated
+ * over scenes.  Outputs (any may be NULL), concatenated over scenes:
+ *   grad_source  n_sources * T floats per scene ([source][t], the layout of
+ *                ard_set_source_series)          dJ/d(source series)
+ *   grad_scale   6 floats per scene, ARD_PML_*   dJ/d(PML face scale)
  *   loss         1 float per scene
- * grad_initial_pressure is read back per partition with
- * ard_read_initial_pressure_grad. */
+ * grad_scale needs forward PML values in reverse order: the forward run
+ * then keeps a copy of the state every `checkpoint_every` steps (<= 0:
+ * chosen to balance checkpoint and history memory) and each segment is run
+ * again before its backward sweep.  Without grad_scale nothing is stored.
+ * dJ/d(initial pressure) of an air partition is read afterwards with
+ * ard_read_initial_pressure_grad (width*height*depth floats, [z][y][x]). */
 int ard_adjoint(ard_ctx* ctx, int64_t T, const float* target,
                 int32_t checkpoint_every,
                 float* grad_source, float* grad_scale, float* loss);
