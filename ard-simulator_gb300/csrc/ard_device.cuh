@@ -134,17 +134,17 @@ struct XformJob {
   double scale;
 };
 
-// One fused 2D transform of a face layer, for output columns [u0, u0 + ub):
-//   T[r][c]   = sum_j X[r][j] B(j, u0 + c)        (along the fast axis U)
-//   Out[o][c] = scale sum_r A(o, r) T[r][c]        (along the slow axis V)
-// X (V x U, row pitch ld) = sum over nparts slabs of in0 + sgn * in1.
+// One fused 2D transform of a pair of face layers, for output columns
+// [u0, u0 + ub):
+//   out0 = scale A (X0 + X1) B,   out1 = scale A (X0 - X1) B
+// X0, X1: V x U, row pitch ld; A: V x V, B: U x U (row-contiguous copies
+// of the transform matrices, restricted to the slab's columns for B).
 // Forward: A = C_V, B(j, u) = C_U[u][j]; inverse: A(o, r) = Ci_V[r][o],
-// B(j, u) = Ci_U[j][u].  tabA / tabB point at row-contiguous copies.
+// B(j, u) = Ci_U[j][u].
 struct Face2DJob {
-  long long in0, in1, out;
-  long long part_stride;
+  long long in0, in1;
+  long long out0, out1;
   long long tabA, tabB;
-  int nparts, sgn;
   int V, U, ld;
   int u0, ub;
   double scale;

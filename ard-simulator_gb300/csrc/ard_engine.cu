@@ -265,6 +265,7 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
       ARD_CUDA(cudaGetLastError());
     }
     ARD_CUDA(mark(kStageInvCols));
+    if (int rc = launch_partial_sums<T>(ctx, s)) return rc;
     if (ctx->fused_faces) {
       face2d_kernel<T><<<grid_for((long long)ctx->inv2d.size(), 1, gx), 256, ctx->f2d_bytes, s>>>(
           buf, ctx->d_inv2d, (int)ctx->inv2d.size(), ctx->f2d_smem);
@@ -295,6 +296,17 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   return ARD_OK;
 }
 
+template <typename T>
+int launch_partial_sums(Ctx* ctx, cudaStream_t s) {
+  if (ctx->psum.empty()) return ARD_OK;
+  partial_sum_kernel<T><<<grid_for(ctx->psum_total, 256, ctx->num_sms * 8), 256, 0, s>>>(
+      reinterpret_cast<T*>(ctx->d_buf), ctx->d_psum, (int)ctx->psum.size(), ctx->psum_total);
+  ARD_CUDA(cudaGetLastError());
+  return ARD_OK;
+}
+
+template int launch_partial_sums<float>(Ctx*, cudaStream_t);
+template int launch_partial_sums<double>(Ctx*, cudaStream_t);
 template int launch_step<float>(Ctx*, int, int, cudaStream_t, cudaStream_t, bool, cudaEvent_t*);
 template int launch_step<double>(Ctx*, int, int, cudaStream_t, cudaStream_t, bool, cudaEvent_t*);
 

@@ -58,6 +58,8 @@ struct Ctx {
   std::vector<int4> tiles;
   JobList fwd1, fwd2, inv1, inv2;           // two-pass GEMM face transforms
   std::vector<Face2DJob> fwd2d, inv2d;      // fused face transforms
+  std::vector<SumJob> psum;                 // partial sums before the inverse transforms
+  long long psum_total = 0;
   bool fused_faces = false;
   Face2DSmem f2d_smem{0, 0, 0};
   size_t f2d_bytes = 0;
@@ -93,6 +95,7 @@ struct Ctx {
   int4* d_tiles = nullptr;
   XformJob *d_fwd1 = nullptr, *d_fwd2 = nullptr, *d_inv1 = nullptr, *d_inv2 = nullptr;
   Face2DJob *d_fwd2d = nullptr, *d_inv2d = nullptr;
+  SumJob* d_psum = nullptr;
   float* d_series = nullptr;
   double* d_hist = nullptr;
   long long* d_t = nullptr;
@@ -118,6 +121,8 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
 int launch_steps_direct(Ctx* ctx, int n, cudaStream_t s);
 int ensure_graph(Ctx* ctx);
 int check_guards(Ctx* ctx);
+template <typename T>
+int launch_partial_sums(Ctx* ctx, cudaStream_t s);
 void build_adjoint_jobs(Ctx* ctx);
 void pml_profile_unit(const Ctx* ctx, int type, int L, std::vector<double>* out);
 template <typename T>

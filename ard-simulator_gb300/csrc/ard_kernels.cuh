@@ -198,48 +198,133 @@ __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, co
 // shared memory, the V-transform writes the output slab.
 // ---------------------------------------------------------------------------
 
-struct Face2DSmem {
-  int xs;  // elements for X (and later A): max(V * xp, V * ap)
-  int bs;  // U * 33
-  int ts;  // V * 33
+// Block-wide copy of n elements, 8 independent loads in flight per thread
+// before any is stored (the staging loops are load-latency bound otherwise).
+template <typename T, typename Load, typename Store>
+__device__ __forceinline__ void staged_copy(int n, Load load, Store store) {
+  constexpr int kU = 8;
+  for (int i0 = threadIdx.x; i0 < n; i0 += 256 * kU) {
+    T v[kU];
+#pragma unroll
+    for (int k = 0; k < kU; ++k) {
+      const int i = i0 + k * 256;
+      v[k] = i < n ? load(i) : (T)0;
+    }
+#pragma unroll
+    for (int k = 0; k < kU; ++k) {
+      const int i = i0 + k * 256;
+      if (i < n) store(i, v[k]);
+    }
+  }
+}
+
+// In-place sum of the per-tile partial slabs of the modal contraction:
+// slab 0 of each job receives the sum of its nb slabs (fixed order).
+struct SumJob {
+  long long base;     // slab 0
+  long long count;    // elements per slab
+  long long stride;   // slab stride
+  long long first;    // first element of this job in the launch's index space
+  int nb;
 };
 
+template <typename T>
+__global__ void __launch_bounds__(256) partial_sum_kernel(T* __restrict__ buf, const SumJob* __restrict__ jobs,
+                                                           int njobs, long long total) {
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].first <= g) lo = mid; else hi = mid - 1;
+    }
+    const SumJob J = jobs[lo];
+    const T* p = buf + J.base + (g - J.first);
+    T v[4] = {0, 0, 0, 0};
+    int b = 0;
+    for (; b + 4 <= J.nb; b += 4) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) v[k] += p[(long long)(b + k) * J.stride];
+    }
+    for (; b < J.nb; ++b) v[0] += p[(long long)b * J.stride];
+    buf[J.base + (g - J.first)] = (v[0] + v[1]) + (v[2] + v[3]);
+  }
+}
+
+struct Face2DSmem {
+  int xs;  // X0 and later A: max(V * xp, V * ap)
+  int x1;  // X1: V * xp
+  int bs;  // B slab: roundup(U, 4) * 33
+  int ts;  // each of T0, T1: V * 33
+};
+
+// One block per (layer pair, 32-column slab): X0, X1 (V x U, row pitch ld)
+// are staged in shared memory with cp.async, combined into E = X0 + X1 and
+// O = X0 - X1, transformed along U for the slab (T = E B, O B) and then along
+// V, giving out0 = scale A (E B) and out1 = scale A (O B) for the slab.
+// Layer pairs are the two layers of the same distance from either face
+// (C(k, n-1-j) = (-1)^k C(k, j)): forward (and the adjoint of the inverse)
+// take the layers and give the even / odd parts, the inverse (and the
+// adjoint of the forward) take the even / odd parts and give the layers.
 template <typename T>
 __global__ void __launch_bounds__(256) face2d_kernel(T* __restrict__ buf, const Face2DJob* __restrict__ jobs,
                                                       int njobs, Face2DSmem sm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* Xs = reinterpret_cast<T*>(smem_raw);
-  T* Bs = Xs + sm.xs;
-  T* Ts = Bs + sm.bs;
+  T* X0 = reinterpret_cast<T*>(smem_raw);
+  T* X1 = X0 + sm.xs;
+  T* Bs = X1 + sm.x1;
+  T* T0 = Bs + sm.bs;
+  T* T1 = T0 + sm.ts;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int jb = blockIdx.x; jb < njobs; jb += gridDim.x) {
     const Face2DJob J = jobs[jb];
     const int V = J.V, U = J.U;
-    const int xp = ((U + 3) & ~3) + 4;
+    const int Up = (U + 3) & ~3;
+    const int xp = Up + 4;
     const int ap = ((V + 3) & ~3) + 4;
     __syncthreads();  // previous job done with shared memory
-    for (int i = tid; i < V * xp; i += 256) {
-      const int r = i / xp, j = i - r * xp;
-      T v = 0;
-      if (j < U) {
-        const long long off = (long long)r * J.ld + j;
-        for (int b = 0; b < J.nparts; ++b) {
-          const long long o = (long long)b * J.part_stride + off;
-          v += buf[J.in0 + o];
-          if (J.in1 >= 0) v += (T)J.sgn * buf[J.in1 + o];
-        }
+    // ---- stage X0, X1 and the B slab (asynchronous) ----
+    const T* g0 = buf + J.in0;
+    const T* g1 = buf + J.in1;
+    if (((U | J.ld) & 3) == 0 && ((J.in0 | J.in1) & 3) == 0) {
+      const int q4 = U >> 2;
+      for (int q = tid; q < V * q4; q += 256) {
+        const int r = q / q4, c = (q - r * q4) * 4;
+        const long long off = (long long)r * J.ld + c;
+        cp_async4(X0 + r * xp + c, g0 + off, true);
+        cp_async4(X1 + r * xp + c, g1 + off, true);
       }
-      Xs[i] = v;
+    } else {
+      for (int i = tid; i < V * U; i += 256) {
+        const int r = i / U, c = i - r * U;
+        const long long off = (long long)r * J.ld + c;
+        cp_async_scalar(X0 + r * xp + c, g0 + off, true);
+        cp_async_scalar(X1 + r * xp + c, g1 + off, true);
+      }
+      for (int i = tid; i < V * (Up - U); i += 256) {  // columns U .. Up-1 read as zero
+        const int r = i / (Up - U), c = U + i - r * (Up - U);
+        X0[r * xp + c] = (T)0;
+        X1[r * xp + c] = (T)0;
+      }
     }
     const T* B = buf + J.tabB;
-    for (int i = tid; i < ((U + 3) & ~3) * 32; i += 256) {
+    for (int i = tid; i < Up * 32; i += 256) {
       const int j = i >> 5, c = i & 31;
-      Bs[j * 33 + c] = (j < U && c < J.ub) ? B[(long long)j * U + J.u0 + c] : (T)0;
+      const bool ok = j < U && c < J.ub;
+      cp_async_scalar(Bs + j * 33 + c, B + (ok ? (long long)j * U + J.u0 + c : 0), ok);
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+    for (int i = tid; i < V * xp; i += 256) {
+      const T a = X0[i], b = X1[i];
+      X0[i] = a + b;
+      X1[i] = a - b;
     }
     __syncthreads();
-    // T = X B (slab): lane = column, warp = row group
+    // ---- along U: T0 = E B, T1 = O B (lane = column, warp = row group) ----
     for (int r0 = warp; r0 < V; r0 += 32) {
-      T acc[4] = {0, 0, 0, 0};
+      T e[4] = {0, 0, 0, 0}, o[4] = {0, 0, 0, 0};
       int rr[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) rr[i] = min(r0 + 8 * i, V - 1);
@@ -248,45 +333,71 @@ __global__ void __launch_bounds__(256) face2d_kernel(T* __restrict__ buf, const 
         const T b2 = Bs[(j + 2) * 33 + lane], b3 = Bs[(j + 3) * 33 + lane];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          T x[4];
-          load4(Xs + rr[i] * xp + j, x);
-          acc[i] += x[0] * b0 + x[1] * b1 + x[2] * b2 + x[3] * b3;
+          T x[4], y[4];
+          load4(X0 + rr[i] * xp + j, x);
+          load4(X1 + rr[i] * xp + j, y);
+          e[i] += x[0] * b0 + x[1] * b1 + x[2] * b2 + x[3] * b3;
+          o[i] += y[0] * b0 + y[1] * b1 + y[2] * b2 + y[3] * b3;
         }
       }
 #pragma unroll
       for (int i = 0; i < 4; ++i)
-        if (r0 + 8 * i < V) Ts[(r0 + 8 * i) * 33 + lane] = acc[i];
+        if (r0 + 8 * i < V) {
+          T0[(r0 + 8 * i) * 33 + lane] = e[i];
+          T1[(r0 + 8 * i) * 33 + lane] = o[i];
+        }
     }
     __syncthreads();
-    // A (V x V, row o contiguous) into the X area
+    // ---- A (V x V, row o contiguous) into the X0 area (asynchronous) ----
     const T* A = buf + J.tabA;
-    for (int i = tid; i < V * ap; i += 256) {
-      const int o = i / ap, r = i - o * ap;
-      Xs[i] = r < V ? A[(long long)o * V + r] : (T)0;
+    if ((V & 3) == 0 && (J.tabA & 3) == 0) {
+      const int a4 = ap >> 2;
+      for (int q = tid; q < V * a4; q += 256) {
+        const int o = q / a4, r = (q - o * a4) * 4;
+        const bool ok = r < V;
+        cp_async4(X0 + o * ap + r, A + (ok ? (long long)o * V + r : 0), ok);
+      }
+    } else {
+      for (int i = tid; i < V * ap; i += 256) {
+        const int o = i / ap, r = i - o * ap;
+        const bool ok = r < V;
+        cp_async_scalar(X0 + i, A + (ok ? (long long)o * V + r : 0), ok);
+      }
     }
+    cp_async_commit();
+    cp_async_wait<0>();
     __syncthreads();
+    // ---- along V: out = scale A T ----
     const T scale = (T)J.scale;
     for (int o0 = warp; o0 < V; o0 += 32) {
-      T acc[4] = {0, 0, 0, 0};
+      T e[4] = {0, 0, 0, 0}, od[4] = {0, 0, 0, 0};
       int oo[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) oo[i] = min(o0 + 8 * i, V - 1);
       for (int r = 0; r < V; r += 4) {
-        const T t0 = Ts[r * 33 + lane];
-        const T t1 = (r + 1 < V) ? Ts[(r + 1) * 33 + lane] : (T)0;
-        const T t2 = (r + 2 < V) ? Ts[(r + 2) * 33 + lane] : (T)0;
-        const T t3 = (r + 3 < V) ? Ts[(r + 3) * 33 + lane] : (T)0;
+        T t[4], u[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const bool ok = r + k < V;
+          t[k] = ok ? T0[(r + k) * 33 + lane] : (T)0;
+          u[k] = ok ? T1[(r + k) * 33 + lane] : (T)0;
+        }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           T a4[4];
-          load4(Xs + oo[i] * ap + r, a4);
-          acc[i] += a4[0] * t0 + a4[1] * t1 + a4[2] * t2 + a4[3] * t3;
+          load4(X0 + oo[i] * ap + r, a4);
+          e[i] += a4[0] * t[0] + a4[1] * t[1] + a4[2] * t[2] + a4[3] * t[3];
+          od[i] += a4[0] * u[0] + a4[1] * u[1] + a4[2] * u[2] + a4[3] * u[3];
         }
       }
       if (lane < J.ub) {
 #pragma unroll
         for (int i = 0; i < 4; ++i)
-          if (o0 + 8 * i < V) buf[J.out + (long long)(o0 + 8 * i) * J.ld + J.u0 + lane] = acc[i] * scale;
+          if (o0 + 8 * i < V) {
+            const long long off = (long long)(o0 + 8 * i) * J.ld + J.u0 + lane;
+            buf[J.out0 + off] = e[i] * scale;
+            buf[J.out1 + off] = od[i] * scale;
+          }
       }
     }
   }
@@ -702,7 +813,7 @@ struct PmlArgs {
 // 3) and of phi_a / phi_b (halo 2 along their own axis) is staged in shared
 // memory per layer; the normal-axis stencils run from a register window.
 template <typename T>
-__global__ void __launch_bounds__(256) pml_kernel(PmlArgs<T> a) {
+__global__ void __launch_bounds__(256, 3) pml_kernel(PmlArgs<T> a) {
   constexpr int TA = 8, TB = 32;
   __shared__ T Ps[TA + 6][TB + 6];
   __shared__ T FA[TA + 4][TB];
@@ -752,26 +863,61 @@ __global__ void __launch_bounds__(256) pml_kernel(PmlArgs<T> a) {
       fw[m] = (inside && ll >= 0 && ll < L) ? fn[ll * lstride + col] : (T)0;
     }
     const T d180 = (T)180 * a.dh * a.dh, d12 = (T)12 * a.dh;
-    for (int l = 0; l < L; ++l) {
+    // tiles of the next layer are fetched into registers while the current
+    // layer computes (3 + 2 + 2 values per thread, plus p(t-2) and the force)
+    T nP[3], nA[2], nB[2], nold = 0, nforce = 0;
+    auto fetch = [&](int l) {
       const T* pl = p + l * lstride;
       const T* fal = fa + l * lstride;
       const T* fbl = fb + l * lstride;
-      __syncthreads();  // previous layer done with the tiles
-      for (int i = threadIdx.x; i < (TA + 6) * (TB + 6); i += 256) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int i = threadIdx.x + 256 * k;
         const int r = i / (TB + 6), c = i - r * (TB + 6);
         const int aa = a0 + r - 3, bb = b0 + c - 3;
-        Ps[r][c] = (aa >= 0 && aa < A && bb >= 0 && bb < B) ? pl[(long long)aa * B + bb] : (T)0;
+        nP[k] = (i < (TA + 6) * (TB + 6) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? pl[(long long)aa * B + bb] : (T)0;
       }
-      for (int i = threadIdx.x; i < (TA + 4) * TB; i += 256) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int i = threadIdx.x + 256 * k;
         const int r = i / TB, c = i - r * TB;
         const int aa = a0 + r - 2, bb = b0 + c;
-        FA[r][c] = (aa >= 0 && aa < A && bb < B) ? fal[(long long)aa * B + bb] : (T)0;
+        nA[k] = (i < (TA + 4) * TB && aa >= 0 && aa < A && bb < B) ? fal[(long long)aa * B + bb] : (T)0;
       }
-      for (int i = threadIdx.x; i < TA * (TB + 4); i += 256) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int i = threadIdx.x + 256 * k;
         const int r = i / (TB + 4), c = i - r * (TB + 4);
         const int aa = a0 + r, bb = b0 + c - 2;
-        FB[r][c] = (aa < A && bb >= 0 && bb < B) ? fbl[(long long)aa * B + bb] : (T)0;
+        nB[k] = (i < TA * (TB + 4) && aa < A && bb >= 0 && bb < B) ? fbl[(long long)aa * B + bb] : (T)0;
       }
+      const int sl = l - P.strip0;
+      nold = inside ? pn[l * lstride + col] : (T)0;
+      nforce = (inside && sl >= 0 && sl < 3) ? force[sl * lstride + col] : (T)0;
+    };
+    auto commit = [&]() {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int i = threadIdx.x + 256 * k;
+        if (i < (TA + 6) * (TB + 6)) Ps[i / (TB + 6)][i % (TB + 6)] = nP[k];
+      }
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int i = threadIdx.x + 256 * k;
+        if (i < (TA + 4) * TB) FA[i / TB][i % TB] = nA[k];
+      }
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int i = threadIdx.x + 256 * k;
+        if (i < TA * (TB + 4)) FB[i / (TB + 4)][i % (TB + 4)] = nB[k];
+      }
+    };
+    fetch(0);
+    for (int l = 0; l < L; ++l) {
+      __syncthreads();  // previous layer done with the tiles
+      commit();
+      const T pold = nold, f = nforce;
+      if (l + 1 < L) fetch(l + 1);
       __syncthreads();
       if (inside) {
         T ln = 0, la = 0, lb = 0;
@@ -796,9 +942,7 @@ __global__ void __launch_bounds__(256) pml_kernel(PmlArgs<T> a) {
         gn /= d12; ga /= d12; gb /= d12;
         const long long I = l * lstride + col;
         const T zn = zeta[l];
-        const T pcur = pw[3], pold = pn[I];
-        const int sl = l - P.strip0;
-        const T f = (sl >= 0 && sl < 3) ? force[sl * lstride + col] : (T)0;
+        const T pcur = pw[3];
         const T t3 = a.c0 * a.c0 * (ln + la + lb);
         const T t4 = -zn * (pcur - pold) / a.dt;
         const T pnew = (T)2 * pcur - pold + a.dt * a.dt * (t3 + t4 + (gn + ga + gb) + f);

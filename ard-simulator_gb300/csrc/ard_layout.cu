@@ -165,25 +165,19 @@ void build_adjoint_jobs(Ctx* ctx) {
       const long long UU = (long long)a.U * a.U, VV = (long long)a.V * a.V;
       for (int u0 = 0; u0 < a.U; u0 += 32) {
         const int ub = std::min(32, a.U - u0);
-        for (int pm = 0; pm < 2; ++pm)
-          for (int n = 0; n < 3; ++n) {
-            Face2DJob j{};
-            j.in0 = a.q + n * LS; j.in1 = a.q + (5 - n) * LS; j.sgn = pm ? -1 : 1;
-            j.nparts = 1; j.part_stride = 0;
-            j.out = a.P + (pm * 3 + n) * LS;
-            j.tabA = a.cV + VV; j.tabB = a.cU + 3 * UU;   // Ci_V, Ci_U^T
-            j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.si;
-            ctx->adj1_2d.push_back(j);
-          }
-        for (int L = 0; L < 6; ++L) {
-          const int n = L < 3 ? L : 5 - L;
-          Face2DJob j{};
-          j.in0 = a.R + n * LS; j.in1 = a.R + (3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
-          j.nparts = a.nb; j.part_stride = 6 * LS;
-          j.out = a.a + L * LS;
-          j.tabA = a.cV + 2 * VV; j.tabB = a.cU;          // C_V^T, C_U
-          j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.sf;
-          ctx->adj2_2d.push_back(j);
+        for (int n = 0; n < 3; ++n) {
+          Face2DJob j{};   // q layers n, 5-n -> P[0][n], P[1][n]
+          j.in0 = a.q + n * LS; j.in1 = a.q + (5 - n) * LS;
+          j.out0 = a.P + n * LS; j.out1 = a.P + (3 + n) * LS;
+          j.tabA = a.cV + VV; j.tabB = a.cU + 3 * UU;   // Ci_V, Ci_U^T
+          j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.si;
+          ctx->adj1_2d.push_back(j);
+          Face2DJob k{};   // summed partials R[n], R[3+n] -> adjoint force layers n, 5-n
+          k.in0 = a.R + n * LS; k.in1 = a.R + (3 + n) * LS;
+          k.out0 = a.a + n * LS; k.out1 = a.a + (5 - n) * LS;
+          k.tabA = a.cV + 2 * VV; k.tabB = a.cU;          // C_V^T, C_U
+          k.V = a.V; k.U = a.U; k.ld = a.ld; k.u0 = u0; k.ub = ub; k.scale = D.sf;
+          ctx->adj2_2d.push_back(k);
         }
       }
       // two-pass GEMM form (partitions whose layers do not fit in shared memory)
@@ -204,7 +198,7 @@ void build_adjoint_jobs(Ctx* ctx) {
         const int n = L < 3 ? L : 5 - L;
         XformJob j{};     // columns along V with C_V^T: A(o, r) = C_V[r][o]
         j.in0 = a.R + (0 * 3 + n) * LS; j.in1 = a.R + (1 * 3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
-        j.nparts = a.nb; j.part_stride = 6 * LS;
+        j.nparts = 1; j.part_stride = 0;   // partials summed beforehand (partial_sum_kernel)
         j.out = a.tmp + L * LS; j.ctab = a.cV; j.n = a.V; j.batch = a.U; j.ld = a.ld;
         j.inverse = 1; j.rows = 0; j.scale = 1.0;
         add_job(ctx->adjg[2], j);
@@ -580,6 +574,19 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     }
   }
 
+  // ---- sums of the modal tiles' contraction partials (slab 0 receives the sum) ----
+  for (const DctDev& D : ctx->dct) {
+    const long long LX = 6LL * D.d * D.h, LY = 6LL * D.d * D.wp, LZ = 6LL * D.h * D.wp;
+    const long long base[3] = {D.RX, D.RY, D.RZ}, cnt[3] = {LX, LY, LZ};
+    const int nb[3] = {D.nbx, D.nby, D.nbz};
+    for (int k = 0; k < 3; ++k) {
+      if (nb[k] < 2) continue;
+      SumJob j{base[k], cnt[k], cnt[k], ctx->psum_total, nb[k]};
+      ctx->psum.push_back(j);
+      ctx->psum_total += cnt[k];
+    }
+  }
+
   // ---- transform jobs (GEMMs over the face layers) ----
   auto add_job = [](JobList& list, XformJob j) {
     const int Md = j.rows ? j.batch : j.n, Nd = j.rows ? j.n : j.batch;
@@ -614,7 +621,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         const int n = L < 3 ? L : 5 - L;
         XformJob j{};
         j.in0 = a.R + (0 * 3 + n) * LS; j.in1 = a.R + (1 * 3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
-        j.nparts = a.nb; j.part_stride = 6 * LS;
+        j.nparts = 1; j.part_stride = 0;   // partials summed beforehand (partial_sum_kernel)
         j.out = a.tmp + L * LS; j.ctab = a.cV + (long long)a.nV * a.nV; j.n = a.nV; j.batch = a.nU; j.ld = a.ld;
         j.inverse = 1; j.rows = 0; j.scale = 1.0;
         add_job(ctx->inv1, j);
@@ -630,45 +637,43 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   // ---- fused face transforms (one kernel per direction) when a layer fits in shared memory ----
   {
     const size_t es0 = elem_size(ctx);
-    long long xs = 0, bs = 0, ts = 0;
+    long long xs = 0, x1 = 0, bs = 0, ts = 0;
     for (const DctDev& D : ctx->dct) {
-      struct Ax { long long f, p, P, R; int U, V, ld; long long cU, cV; int nb; };
-      const Ax axes[3] = {{D.fX, D.pX, D.PX, D.RX, D.h, D.d, D.h, D.ch, D.cd, D.nbx},
-                          {D.fY, D.pY, D.PY, D.RY, D.w, D.d, D.wp, D.cw, D.cd, D.nby},
-                          {D.fZ, D.pZ, D.PZ, D.RZ, D.w, D.h, D.wp, D.cw, D.ch, D.nbz}};
+      struct Ax { long long f, p, P, R; int U, V, ld; long long cU, cV; };
+      const Ax axes[3] = {{D.fX, D.pX, D.PX, D.RX, D.h, D.d, D.h, D.ch, D.cd},
+                          {D.fY, D.pY, D.PY, D.RY, D.w, D.d, D.wp, D.cw, D.cd},
+                          {D.fZ, D.pZ, D.PZ, D.RZ, D.w, D.h, D.wp, D.cw, D.ch}};
       for (const Ax& a : axes) {
         const long long LS = (long long)a.V * a.ld;
         const long long UU = (long long)a.U * a.U, VV = (long long)a.V * a.V;
-        xs = std::max(xs, std::max((long long)a.V * (((a.U + 3) & ~3) + 4), (long long)a.V * (((a.V + 3) & ~3) + 4)));
+        const long long xp = ((a.U + 3) & ~3) + 4, ap = ((a.V + 3) & ~3) + 4;
+        xs = std::max(xs, std::max((long long)a.V * xp, (long long)a.V * ap));
+        x1 = std::max(x1, (long long)a.V * xp);
         bs = std::max(bs, (long long)((a.U + 3) & ~3) * 33);
         ts = std::max(ts, (long long)a.V * 33);
         for (int u0 = 0; u0 < a.U; u0 += 32) {
           const int ub = std::min(32, a.U - u0);
-          for (int pm = 0; pm < 2; ++pm)
-            for (int n = 0; n < 3; ++n) {
-              Face2DJob j{};
-              j.in0 = a.f + n * LS; j.in1 = a.f + (5 - n) * LS; j.sgn = pm ? -1 : 1;
-              j.nparts = 1; j.part_stride = 0;
-              j.out = a.P + (pm * 3 + n) * LS;
-              j.tabA = a.cV; j.tabB = a.cU + 2 * UU;
-              j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.sf;
-              ctx->fwd2d.push_back(j);
-            }
-          for (int L = 0; L < 6; ++L) {
-            const int n = L < 3 ? L : 5 - L;
+          for (int n = 0; n < 3; ++n) {
+            // forward: layers n, 5-n -> even / odd parts P[0][n], P[1][n]
             Face2DJob j{};
-            j.in0 = a.R + n * LS; j.in1 = a.R + (3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
-            j.nparts = a.nb; j.part_stride = 6 * LS;
-            j.out = a.p + L * LS;
-            j.tabA = a.cV + 3 * VV; j.tabB = a.cU + UU;
-            j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.si;
-            ctx->inv2d.push_back(j);
+            j.in0 = a.f + n * LS; j.in1 = a.f + (5 - n) * LS;
+            j.out0 = a.P + n * LS; j.out1 = a.P + (3 + n) * LS;
+            j.tabA = a.cV; j.tabB = a.cU + 2 * UU;
+            j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.sf;
+            ctx->fwd2d.push_back(j);
+            // inverse: even / odd parts (partials summed beforehand) -> layers n, 5-n
+            Face2DJob k{};
+            k.in0 = a.R + n * LS; k.in1 = a.R + (3 + n) * LS;
+            k.out0 = a.p + n * LS; k.out1 = a.p + (5 - n) * LS;
+            k.tabA = a.cV + 3 * VV; k.tabB = a.cU + UU;
+            k.V = a.V; k.U = a.U; k.ld = a.ld; k.u0 = u0; k.ub = ub; k.scale = D.si;
+            ctx->inv2d.push_back(k);
           }
         }
       }
     }
-    ctx->f2d_smem = Face2DSmem{(int)xs, (int)bs, (int)ts};
-    ctx->f2d_bytes = (size_t)(xs + bs + ts) * es0;
+    ctx->f2d_smem = Face2DSmem{(int)xs, (int)x1, (int)bs, (int)ts};
+    ctx->f2d_bytes = (size_t)(xs + x1 + bs + 2 * ts) * es0;
     ctx->fused_faces = !ctx->dct.empty() && ctx->f2d_bytes <= (size_t)std::min(ctx->smem_optin, 200 * 1024);
   }
   if (ctx->adjoint) build_adjoint_jobs(ctx);
@@ -712,6 +717,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   if ((rc = up(&ctx->d_inv2, ctx->inv2.jobs))) return rc;
   if ((rc = up(&ctx->d_fwd2d, ctx->fwd2d))) return rc;
   if ((rc = up(&ctx->d_inv2d, ctx->inv2d))) return rc;
+  if ((rc = up(&ctx->d_psum, ctx->psum))) return rc;
   if (ctx->adjoint) {
     if ((rc = up(&ctx->d_adj1_2d, ctx->adj1_2d))) return rc;
     if ((rc = up(&ctx->d_adj2_2d, ctx->adj2_2d))) return rc;
@@ -769,7 +775,7 @@ void free_ctx_device(Ctx* ctx) {
                   ctx->d_recpts, ctx->d_tiles, ctx->d_fwd1, ctx->d_fwd2, ctx->d_inv1, ctx->d_inv2, ctx->d_fwd2d,
                   ctx->d_inv2d, ctx->d_series,
                   ctx->d_hist, ctx->d_t, ctx->d_adj1_2d, ctx->d_adj2_2d, ctx->d_adjg[0], ctx->d_adjg[1],
-                  ctx->d_adjg[2], ctx->d_adjg[3], ctx->d_tb, ctx->d_phist};
+                  ctx->d_adjg[2], ctx->d_adjg[3], ctx->d_tb, ctx->d_phist, ctx->d_psum};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
