@@ -105,6 +105,7 @@ SIGNATURES = {
     "ard_adjoint": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float),
                               C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "ard_read_initial_pressure_grad": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
+    "ard_kernels_per_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ard_profile_steps": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "ard_last_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
 }
@@ -191,6 +192,20 @@ class Scene:
     @property
     def pml_cells(self):
         return sum(p[5] * p[6] * p[7] for p in self.partitions if p[0] == PART_PML)
+
+    @property
+    def face_cells(self):
+        """Interface face cells (each reads 6 and writes 6 values per step)."""
+        n = 0
+        for b in self.boundaries:
+            t, xs, xe, ys, ye, zs, ze = b[0], b[3], b[4], b[5], b[6], b[7], b[8]
+            if t == 0:
+                n += max(0, ye - ys) * max(0, ze - zs)
+            elif t == 1:
+                n += max(0, xe - xs) * max(0, ze - zs)
+            else:
+                n += max(0, xe - xs) * max(0, ye - ys)
+        return n
 
 
 def _params(dh, dt, c0, pml_layers, absorption=1.0, pml_R=0.0, modal_damping=0.0):
@@ -309,6 +324,12 @@ class Simulation:
 
     def synchronize(self):
         self._c(lib().ard_synchronize(self._h))
+
+    @property
+    def kernels_per_step(self):
+        v = C.c_int32()
+        self._c(lib().ard_kernels_per_step(self._h, C.byref(v)))
+        return v.value
 
     @property
     def time_step(self):

@@ -65,7 +65,8 @@ int configure_adjoint(Ctx* ctx) {
   ARD_CUDA(cudaFuncSetAttribute(modal_kernel<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, msmem));
   ARD_CUDA(cudaFuncSetAttribute(modal_kernel<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, msmem));
   if (ctx->fused_faces)
-    ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->f2d_bytes));
+    ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  std::max(ctx->smem_optin, (int)ctx->f2d_bytes)));
   return ARD_OK;
 }
 
@@ -108,7 +109,7 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
   if (!ctx->dct.empty()) {
     const int gx = ctx->num_sms * 4;
     if (ctx->fused_faces) {
-      face2d_kernel<T><<<grid_for((long long)ctx->adj1_2d.size(), 1, gx), 256, ctx->f2d_bytes, s>>>(
+      face2d_kernel<T><<<grid_for((long long)ctx->adj1_2d.size(), 1, gx), kFace2DThreads, ctx->f2d_bytes, s>>>(
           buf, ctx->d_adj1_2d, (int)ctx->adj1_2d.size(), ctx->f2d_smem);
     } else {
       for (int k = 0; k < 2; ++k)
@@ -132,7 +133,7 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
     }
     if (int rc2 = launch_partial_sums<T>(ctx, s)) return rc2;
     if (ctx->fused_faces) {
-      face2d_kernel<T><<<grid_for((long long)ctx->adj2_2d.size(), 1, gx), 256, ctx->f2d_bytes, s>>>(
+      face2d_kernel<T><<<grid_for((long long)ctx->adj2_2d.size(), 1, gx), kFace2DThreads, ctx->f2d_bytes, s>>>(
           buf, ctx->d_adj2_2d, (int)ctx->adj2_2d.size(), ctx->f2d_smem);
     } else {
       for (int k = 2; k < 4; ++k)

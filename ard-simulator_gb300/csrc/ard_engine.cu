@@ -90,7 +90,10 @@ static int validate_scene(const ard_scene& s, std::string* err) {
 // modal kernel needs more than 48 KB of dynamic shared memory.
 static int configure_kernels(Ctx* ctx) {
   const int modal_smem = (int)(kModalSmemElems * elem_size(ctx));
-  const int f2d = (int)std::max<size_t>(ctx->f2d_bytes, 1);
+  // The attribute belongs to the kernel, process-wide, not to the context:
+  // set the device's opt-in maximum so that contexts with different layer
+  // sizes can be interleaved in one process.
+  const int f2d = std::max(ctx->smem_optin, (int)ctx->f2d_bytes);
   if (ctx->prec == ARD_PREC_F64) {
     ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
     ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
@@ -177,6 +180,21 @@ extern "C" int ard_last_error(const ard_ctx* c, char* buf, int64_t n) {
   return ARD_OK;
 }
 
+extern "C" int ard_kernels_per_step(const ard_ctx* c, int32_t* out) {
+  if (!c || !out) return ARD_ERR_INVALID;
+  const Ctx* ctx = reinterpret_cast<const Ctx*>(c);
+  int n = ctx->pml_blocks.empty() ? 0 : 1;
+  if (!ctx->dct.empty()) {
+    n += ctx->fused_faces ? 2 : 4;           // forward and inverse face transforms
+    n += 1;                                  // modal update
+    n += ctx->recpts.empty() ? 0 : 1;        // recorder sums
+    n += ctx->psum.empty() ? 0 : 1;          // partial sums
+  }
+  n += ctx->n_face_cells > 0 ? 1 : 0;        // interfaces
+  *out = n;
+  return ARD_OK;
+}
+
 extern "C" int ard_time_step(const ard_ctx* c, int64_t* out) {
   if (!c || !out) return ARD_ERR_INVALID;
   *out = reinterpret_cast<const Ctx*>(c)->t_host;
@@ -235,7 +253,7 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
     const int gx = ctx->num_sms * 4;
     ARD_CUDA(mark(kStageFwdRows));
     if (ctx->fused_faces) {
-      face2d_kernel<T><<<grid_for((long long)ctx->fwd2d.size(), 1, gx), 256, ctx->f2d_bytes, s>>>(
+      face2d_kernel<T><<<grid_for((long long)ctx->fwd2d.size(), 1, gx), kFace2DThreads, ctx->f2d_bytes, s>>>(
           buf, ctx->d_fwd2d, (int)ctx->fwd2d.size(), ctx->f2d_smem);
     } else {
       xform_gemm_kernel<T><<<grid_for(ctx->fwd1.units, 1, gx), 256, 0, s>>>(buf, ctx->d_fwd1, (int)ctx->fwd1.jobs.size(),
@@ -267,7 +285,7 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
     ARD_CUDA(mark(kStageInvCols));
     if (int rc = launch_partial_sums<T>(ctx, s)) return rc;
     if (ctx->fused_faces) {
-      face2d_kernel<T><<<grid_for((long long)ctx->inv2d.size(), 1, gx), 256, ctx->f2d_bytes, s>>>(
+      face2d_kernel<T><<<grid_for((long long)ctx->inv2d.size(), 1, gx), kFace2DThreads, ctx->f2d_bytes, s>>>(
           buf, ctx->d_inv2d, (int)ctx->inv2d.size(), ctx->f2d_smem);
     } else {
       xform_gemm_kernel<T><<<grid_for(ctx->inv1.units, 1, gx), 256, 0, s>>>(buf, ctx->d_inv1, (int)ctx->inv1.jobs.size(),

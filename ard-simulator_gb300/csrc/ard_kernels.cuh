@@ -198,26 +198,6 @@ __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, co
 // shared memory, the V-transform writes the output slab.
 // ---------------------------------------------------------------------------
 
-// Block-wide copy of n elements, 8 independent loads in flight per thread
-// before any is stored (the staging loops are load-latency bound otherwise).
-template <typename T, typename Load, typename Store>
-__device__ __forceinline__ void staged_copy(int n, Load load, Store store) {
-  constexpr int kU = 8;
-  for (int i0 = threadIdx.x; i0 < n; i0 += 256 * kU) {
-    T v[kU];
-#pragma unroll
-    for (int k = 0; k < kU; ++k) {
-      const int i = i0 + k * 256;
-      v[k] = i < n ? load(i) : (T)0;
-    }
-#pragma unroll
-    for (int k = 0; k < kU; ++k) {
-      const int i = i0 + k * 256;
-      if (i < n) store(i, v[k]);
-    }
-  }
-}
-
 // In-place sum of the per-tile partial slabs of the modal contraction:
 // slab 0 of each job receives the sum of its nb slabs (fixed order).
 struct SumJob {
@@ -251,6 +231,8 @@ __global__ void __launch_bounds__(256) partial_sum_kernel(T* __restrict__ buf, c
   }
 }
 
+constexpr int kFace2DThreads = 512;
+
 struct Face2DSmem {
   int xs;  // X0 and later A: max(V * xp, V * ap)
   int x1;  // X1: V * xp
@@ -267,7 +249,7 @@ struct Face2DSmem {
 // take the layers and give the even / odd parts, the inverse (and the
 // adjoint of the forward) take the even / odd parts and give the layers.
 template <typename T>
-__global__ void __launch_bounds__(256) face2d_kernel(T* __restrict__ buf, const Face2DJob* __restrict__ jobs,
+__global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ buf, const Face2DJob* __restrict__ jobs,
                                                       int njobs, Face2DSmem sm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* X0 = reinterpret_cast<T*>(smem_raw);
@@ -276,6 +258,9 @@ __global__ void __launch_bounds__(256) face2d_kernel(T* __restrict__ buf, const 
   T* T0 = Bs + sm.bs;
   T* T1 = T0 + sm.ts;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // warps in groups of 8: a group covers 32 consecutive rows (4 per warp, stride 8)
+  constexpr int kRowStep = 32 * (kFace2DThreads / 256);
+  const int wrow = (warp & 7) + 32 * (warp >> 3);
   for (int jb = blockIdx.x; jb < njobs; jb += gridDim.x) {
     const Face2DJob J = jobs[jb];
     const int V = J.V, U = J.U;
@@ -288,27 +273,27 @@ __global__ void __launch_bounds__(256) face2d_kernel(T* __restrict__ buf, const 
     const T* g1 = buf + J.in1;
     if (((U | J.ld) & 3) == 0 && ((J.in0 | J.in1) & 3) == 0) {
       const int q4 = U >> 2;
-      for (int q = tid; q < V * q4; q += 256) {
+      for (int q = tid; q < V * q4; q += kFace2DThreads) {
         const int r = q / q4, c = (q - r * q4) * 4;
         const long long off = (long long)r * J.ld + c;
         cp_async4(X0 + r * xp + c, g0 + off, true);
         cp_async4(X1 + r * xp + c, g1 + off, true);
       }
     } else {
-      for (int i = tid; i < V * U; i += 256) {
+      for (int i = tid; i < V * U; i += kFace2DThreads) {
         const int r = i / U, c = i - r * U;
         const long long off = (long long)r * J.ld + c;
         cp_async_scalar(X0 + r * xp + c, g0 + off, true);
         cp_async_scalar(X1 + r * xp + c, g1 + off, true);
       }
-      for (int i = tid; i < V * (Up - U); i += 256) {  // columns U .. Up-1 read as zero
+      for (int i = tid; i < V * (Up - U); i += kFace2DThreads) {  // columns U .. Up-1 read as zero
         const int r = i / (Up - U), c = U + i - r * (Up - U);
         X0[r * xp + c] = (T)0;
         X1[r * xp + c] = (T)0;
       }
     }
     const T* B = buf + J.tabB;
-    for (int i = tid; i < Up * 32; i += 256) {
+    for (int i = tid; i < Up * 32; i += kFace2DThreads) {
       const int j = i >> 5, c = i & 31;
       const bool ok = j < U && c < J.ub;
       cp_async_scalar(Bs + j * 33 + c, B + (ok ? (long long)j * U + J.u0 + c : 0), ok);
@@ -316,14 +301,14 @@ __global__ void __launch_bounds__(256) face2d_kernel(T* __restrict__ buf, const 
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
-    for (int i = tid; i < V * xp; i += 256) {
+    for (int i = tid; i < V * xp; i += kFace2DThreads) {
       const T a = X0[i], b = X1[i];
       X0[i] = a + b;
       X1[i] = a - b;
     }
     __syncthreads();
     // ---- along U: T0 = E B, T1 = O B (lane = column, warp = row group) ----
-    for (int r0 = warp; r0 < V; r0 += 32) {
+    for (int r0 = wrow; r0 < V; r0 += kRowStep) {
       T e[4] = {0, 0, 0, 0}, o[4] = {0, 0, 0, 0};
       int rr[4];
 #pragma unroll
@@ -352,13 +337,13 @@ __global__ void __launch_bounds__(256) face2d_kernel(T* __restrict__ buf, const 
     const T* A = buf + J.tabA;
     if ((V & 3) == 0 && (J.tabA & 3) == 0) {
       const int a4 = ap >> 2;
-      for (int q = tid; q < V * a4; q += 256) {
+      for (int q = tid; q < V * a4; q += kFace2DThreads) {
         const int o = q / a4, r = (q - o * a4) * 4;
         const bool ok = r < V;
         cp_async4(X0 + o * ap + r, A + (ok ? (long long)o * V + r : 0), ok);
       }
     } else {
-      for (int i = tid; i < V * ap; i += 256) {
+      for (int i = tid; i < V * ap; i += kFace2DThreads) {
         const int o = i / ap, r = i - o * ap;
         const bool ok = r < V;
         cp_async_scalar(X0 + i, A + (ok ? (long long)o * V + r : 0), ok);
@@ -369,7 +354,7 @@ __global__ void __launch_bounds__(256) face2d_kernel(T* __restrict__ buf, const 
     __syncthreads();
     // ---- along V: out = scale A T ----
     const T scale = (T)J.scale;
-    for (int o0 = warp; o0 < V; o0 += 32) {
+    for (int o0 = wrow; o0 < V; o0 += kRowStep) {
       T e[4] = {0, 0, 0, 0}, od[4] = {0, 0, 0, 0};
       int oo[4];
 #pragma unroll
@@ -559,6 +544,27 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
     const T* tabB = buf + D.tabB;
     const T damping = (T)D.damping;
 
+    // this thread's ky-contraction outputs: up to 3 of the 6 KXT (parity, row, kx) columns
+    const int rmax = min(RPC, h - ky0);
+    // (slot offset | first row << 16, or -1; output offset from RY, 32-bit)
+    int yo[3], yg[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int o = tid + q * kModalThreads;
+      yo[q] = -1; yg[q] = 0;
+      if (o < 6 * KXT) {
+        const int pm = o / (3 * KXT);
+        const int rem = o - pm * 3 * KXT;
+        const int n = rem / KXT, kl = rem - n * KXT;
+        const int kx = tl.y * KXT + kl;
+        if (kx < wp) {
+          yo[q] = (n * 1024 + kl) | ((((ky0 & 1) == pm) ? 0 : 1) << 16);
+          yg[q] = (int)(((long long)tl.z * 6 + pm * 3 + n) * planeY + kx);
+        }
+      }
+    }
+    T* const RYb = buf + D.RY;
+
     // per-plane inputs of plane kz into stage buffer sb (asynchronous)
     auto issue = [&](int kz, int sb) {
       T* st = stage + sb * kModalStage;
@@ -701,15 +707,13 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
       }
       __syncthreads();
       // ky contraction of this kz: sum the tile's rows of matching parity
-      for (int o = tid; o < 6 * KXT; o += kModalThreads) {
-        const int pm = o / (3 * KXT);
-        const int rem = o - pm * 3 * KXT;
-        const int n = rem / KXT, kl = rem - n * KXT;
-        const int kx = tl.y * KXT + kl;
-        if (kx >= wp) continue;
-        T s = 0;
-        for (int r = ((ky0 & 1) == pm) ? 0 : 1; r < RPC && ky0 + r < h; r += 2) s += slot[n * 1024 + r * KXT + kl];
-        buf[D.RY + ((long long)tl.z * 6 + pm * 3 + n) * planeY + (long long)kz * wp + kx] = s;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        if (yo[q] < 0) continue;
+        const int so = yo[q] & 0xffff;
+        T sum = 0;
+        for (int r = yo[q] >> 16; r < rmax; r += 2) sum += slot[so + r * KXT];
+        RYb[yg[q] + kz * wp] = sum;
       }
     };
 
@@ -813,7 +817,7 @@ struct PmlArgs {
 // 3) and of phi_a / phi_b (halo 2 along their own axis) is staged in shared
 // memory per layer; the normal-axis stencils run from a register window.
 template <typename T>
-__global__ void __launch_bounds__(256, 3) pml_kernel(PmlArgs<T> a) {
+__global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
   constexpr int TA = 8, TB = 32;
   __shared__ T Ps[TA + 6][TB + 6];
   __shared__ T FA[TA + 4][TB];
@@ -862,7 +866,7 @@ __global__ void __launch_bounds__(256, 3) pml_kernel(PmlArgs<T> a) {
       const int ll = m - 2;
       fw[m] = (inside && ll >= 0 && ll < L) ? fn[ll * lstride + col] : (T)0;
     }
-    const T d180 = (T)180 * a.dh * a.dh, d12 = (T)12 * a.dh;
+    const T r180 = (T)1 / ((T)180 * a.dh * a.dh), r12 = (T)1 / ((T)12 * a.dh), rdt = (T)1 / a.dt;
     // tiles of the next layer are fetched into registers while the current
     // layer computes (3 + 2 + 2 values per thread, plus p(t-2) and the force)
     T nP[3], nA[2], nB[2], nold = 0, nforce = 0;
@@ -937,14 +941,14 @@ __global__ void __launch_bounds__(256, 3) pml_kernel(PmlArgs<T> a) {
           ga += c5[m] * FA[ta + m][tb];
           gb += c5[m] * FB[ta][tb + m];
         }
-        ln /= d180; la /= d180; lb /= d180;
-        un /= d12; ua /= d12; ub /= d12;
-        gn /= d12; ga /= d12; gb /= d12;
+        ln *= r180; la *= r180; lb *= r180;
+        un *= r12; ua *= r12; ub *= r12;
+        gn *= r12; ga *= r12; gb *= r12;
         const long long I = l * lstride + col;
         const T zn = zeta[l];
         const T pcur = pw[3];
         const T t3 = a.c0 * a.c0 * (ln + la + lb);
-        const T t4 = -zn * (pcur - pold) / a.dt;
+        const T t4 = -zn * (pcur - pold) * rdt;
         const T pnew = (T)2 * pcur - pold + a.dt * a.dt * (t3 + t4 + (gn + ga + gb) + f);
         pn[I] = pnew;
         const T fnc = fw[2];

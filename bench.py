@@ -19,6 +19,13 @@ extra work, not counted.
           against the measured HBM copy bandwidth
   cpu_baseline  the oracle (C restatement of the reference's CPU solver,
           FP32, OpenMP over partitions) on a bounded sample of the same scene
+  adjoint the forward + adjoint of the recorder misfit on the same workload
+          (gradients w.r.t. source series, initial pressure and the six PML
+          face scales; target from a seeded perturbed source, face scales
+          U(0.5, 1.5), checkpoints every 64 steps): wall time against the
+          forward alone, and Gcell-steps/s of forward + adjoint
+  --plain runs every scene in its own context one after another (the
+          per-scene path) instead of one batched context
 
 Multi-GPU (torchrun): scenes are independent, so ranks shard the scene list
 (c2) or run replicas (single-scene configs); no collective touches the data
@@ -59,11 +66,12 @@ def peaks():
 
 def workload(name, sim_steps=None, rank=0, world=1):
     from ard_gb300 import configs as K
+    from ard_gb300 import shard
     cfg = K.config(name, steps=sim_steps)
     scenes = cfg["scenes"]
-    if len(scenes) > 1 and world > 1:
-        scenes = scenes[rank::world]      # independent scenes: shard, weak scaling by scene count
-    cfg["scenes"] = scenes
+    # independent scenes: balanced shards by air cells (a single scene is replicated)
+    costs = [sum(b[3] * b[4] * b[5] for b in sc["air"]) for sc in scenes]
+    cfg["scenes"] = [scenes[i] for i in shard.local_scenes(costs, rank, world)]
     return cfg
 
 
@@ -173,6 +181,67 @@ def run_reference_arm(args, rank):
     return 0
 
 
+def adjoint_measurement(A, cfg, scenes, args, device):
+    """Forward + adjoint of the recorder misfit (gradients w.r.t. the source
+    series, the initial pressure and the six PML face scales) against the
+    forward alone, on the bench workload.  Target: recorders of a run whose
+    sources carry seeded band-limited noise on top of the series; face scales
+    U(0.5, 1.5), seeded."""
+    import torch
+    S = args.adjoint_steps or cfg["steps"]
+    rng = np.random.default_rng(7)
+    sim = A.Simulation(scenes, max_steps=S, device=device, adjoint=True)
+    n_src = sum(len(sc["sources"]) for sc in cfg["scenes"])
+    series = np.zeros((n_src, S), np.float32)
+    k = 0
+    for sc in cfg["scenes"]:
+        for s in sc["series"]:
+            series[k] = s[:S]
+            k += 1
+    amp = float(np.abs(series).max()) or 1.0
+    noise = rng.standard_normal((n_src, S))
+    spec = np.fft.rfft(noise, axis=1)
+    f = np.fft.rfftfreq(S, d=cfg["dt"])
+    spec[:, f > 2000.0] = 0                      # 2 kHz band limit
+    pert = (0.1 * amp * np.fft.irfft(spec, n=S, axis=1) / (np.abs(np.fft.irfft(spec, n=S, axis=1)).max() + 1e-30))
+    pert[:, 1024:] = 0                           # 1024 samples of noise, then zeros
+    scales = rng.uniform(0.5, 1.5, size=(len(scenes), 6)).astype(np.float32)
+
+    def load(series_):
+        sim.reset()
+        sim._c(A.lib().ard_set_source_series(sim._h, -1, -1, A._fptr(np.ascontiguousarray(series_, np.float32)), S))
+        for i in range(len(scenes)):
+            sim.set_pml_scale(scales[i], scene=i)
+
+    load(series + pert.astype(np.float32))
+    sim.run(S)
+    target = sim.recorders(scene=-1)
+    tparts, r0 = [], 0
+    for sc in cfg["scenes"]:
+        n = len(sc["recorders"])
+        tparts.append(target[:, r0:r0 + n])
+        r0 += n
+    load(series)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.run(S)
+    sim.synchronize()
+    fwd_s = time.perf_counter() - t0
+    load(series)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g = sim.adjoint(S, tparts, checkpoint_every=args.checkpoint_every, want_scale=True)
+    adj_s = time.perf_counter() - t0
+    n_air = sum(s.air_cells for s in scenes)
+    out = {"workload": f"{cfg['name']} geometry, {S} steps, checkpoint every {args.checkpoint_every}",
+           "fwd_s": fwd_s, "fwd_adj_s": adj_s, "ratio": adj_s / fwd_s,
+           "value": n_air * S / adj_s / 1e9, "unit": UNIT,
+           "loss": float(np.sum(g["loss"])),
+           "grad_scale_scene0": [float(v) for v in g["grad_scale"][0]]}
+    sim.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -184,6 +253,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=10, help="time steps of the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=6, help="time steps per reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=None, help="steps of the adjoint measurement (default: sim steps)")
+    ap.add_argument("--checkpoint-every", type=int, default=64)
+    ap.add_argument("--plain", action="store_true", help="one context per scene, run one after another")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
@@ -211,7 +284,8 @@ def main():
     n_pml = sum(s.pml_cells for s in scenes)
     n_src = sum(len(sc["sources"]) for sc in cfg["scenes"])
     n_rec = sum(len(sc["recorders"]) for sc in cfg["scenes"])
-    sim = A.Simulation(scenes, max_steps=S, device=local)
+    sims = [A.Simulation([sc], max_steps=S, device=local) for sc in scenes] if args.plain else None
+    sim = sims[0] if args.plain else A.Simulation(scenes, max_steps=S, device=local)
     series = np.zeros((n_src, S), np.float32)
     k = 0
     for sc in cfg["scenes"]:
@@ -223,11 +297,36 @@ def main():
     import ctypes as C
     fptr = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_float))
 
+    if args.plain:
+        # per-scene contexts: each takes its own rows of the series / recorder buffers
+        src_off = np.cumsum([0] + [len(sc["sources"]) for sc in cfg["scenes"]])
+        rec_off = np.cumsum([0] + [len(sc["recorders"]) for sc in cfg["scenes"]])
+        rec_rows = [torch.empty((S, int(rec_off[i + 1] - rec_off[i])), dtype=torch.float32).pin_memory()
+                    for i in range(len(sims))]
+
     def upload():
-        sim._c(A.lib().ard_set_source_series(sim._h, -1, -1, fptr(pinned_series), S))
+        if not args.plain:
+            sim._c(A.lib().ard_set_source_series(sim._h, -1, -1, fptr(pinned_series), S))
+            return
+        for i, sm in enumerate(sims):
+            if src_off[i + 1] > src_off[i]:
+                sm._c(A.lib().ard_set_source_series(sm._h, -1, -1, fptr(pinned_series[int(src_off[i]):]), S))
 
     def readback():
-        sim._c(A.lib().ard_read_recorders(sim._h, -1, fptr(pinned_rec), 0, S))
+        if not args.plain:
+            sim._c(A.lib().ard_read_recorders(sim._h, -1, fptr(pinned_rec), 0, S))
+            return
+        for i, sm in enumerate(sims):
+            if rec_off[i + 1] > rec_off[i]:
+                sm._c(A.lib().ard_read_recorders(sm._h, -1, fptr(rec_rows[i]), 0, S))
+
+    def reset_all():
+        for sm in (sims if args.plain else [sim]):
+            sm.reset()
+
+    def run_all(n, stream=None):
+        for sm in (sims if args.plain else [sim]):
+            sm.run(n, stream=stream)
 
     upload()
     stream = torch.cuda.Stream()
@@ -235,10 +334,10 @@ def main():
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MiB > 129 MB L2
 
     def simulate():
-        sim.reset()
+        reset_all()
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
-        sim.run(S, stream=handle)
+        run_all(S, stream=handle)
 
     for _ in range(args.warmup):
         simulate()
@@ -252,13 +351,13 @@ def main():
     clocks.start()
     total_ms = 0.0
     for _ in range(args.steps):
-        sim.reset()
+        reset_all()
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-        sim.run(S, stream=handle)
+        run_all(S, stream=handle)
         with torch.cuda.stream(stream):
             e1.record(stream)
         e1.synchronize()
@@ -284,8 +383,8 @@ def main():
     t0 = time.perf_counter()
     for _ in range(args.steps):
         upload()
-        sim.reset()
-        sim.run(S)
+        reset_all()
+        run_all(S)
         readback()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
@@ -315,11 +414,14 @@ def main():
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "kernel": "modal_kernel<float>", "algorithmic_bytes_per_launch": alg_bytes,
                 "launch_ms": modal_ms}
-    step_ms = sum(stages.values())
-    step_bytes = 28 * n_air + 44 * n_pml + 48 * sum(
-        (b[4] - b[3]) * (b[6] - b[5]) if b[0] == 0 else ((b[4] - b[3]) * (b[8] - b[7]) if b[0] == 1 else
-                                                          (b[4] - b[3]) * (b[6] - b[5]))
-        for s in scenes for b in s.boundaries) if False else None
+    # whole step: the reference's per-step algorithmic bytes over the device time of one step
+    n_face = sum(s.face_cells for s in scenes)
+    step_bytes = 28 * n_air + 44 * n_pml + 48 * n_face
+    step_roofline = {"algorithmic_bytes_per_step": step_bytes, "ms_per_step": ms_per_step / S,
+                     "achieved": step_bytes / (ms_per_step / S / 1e3) / 1e9, "unit": "GB/s",
+                     "frac": step_bytes / (ms_per_step / S / 1e3) / 1e9 / peak}
+    kps = sum(sm.kernels_per_step for sm in (sims if args.plain else [sim]))
+    launches = int(args.steps * (S * kps + (S // 32 + S % 32) * (len(sims) if args.plain else 1)))
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -328,10 +430,16 @@ def main():
                        "scenes_per_rank": len(scenes), "parallelism": "replicas" if len(cfg["scenes"]) == 1 else "scene shards",
                        "l2": "flushed (256 MiB write) before every timed simulation; the scene's working set may fit in L2 within a simulation"},
             "roofline": roofline,
+            "step_roofline": step_roofline,
             "stage_ms_per_step": stages,
             "e2e": e2e,
-            "gpu_launches": int(args.steps * (S * 8 + (S + 31) // 32)),
+            "gpu_launches": launches,
+            "kernels_per_step": kps,
             "clocks": clk}
+    if args.plain:
+        line["config"]["parallelism"] = "plain: one context per scene, run one after another"
+    if not args.no_adjoint and not args.plain:
+        line["adjoint"] = adjoint_measurement(A, cfg, scenes, args, local)
     if rank == 0 and not args.no_cpu_baseline:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
         line["cpu_baseline"] = cpu_baseline(cfg, args.cpu_sample)

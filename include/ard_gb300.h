@@ -290,6 +290,11 @@ int ard_profile_steps(ard_ctx* ctx, int64_t nsteps, void* stream, float* stage_m
 /* Message of the last error on this context (NULL ctx: last create error). */
 int ard_last_error(const ard_ctx* ctx, char* buf, int64_t n);
 
+/* Introspection, no counterpart in the reference: number of kernels one
+ * step launches (the step's CUDA graph holds this many kernel nodes per
+ * step, plus one counter kernel per 32 steps). */
+int ard_kernels_per_step(const ard_ctx* ctx, int32_t* out);
+
 /* Library version / ABI check. */
 int ard_abi_version(void);
 

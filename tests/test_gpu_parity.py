@@ -182,3 +182,23 @@ def test_errors_are_reported():
         sim.set_initial_pressure(0, np.zeros((20, 20, 20), np.float32))  # after stepping: state error
     with pytest.raises(A.ArdError):
         sim.field(99)
+
+
+def test_contexts_with_different_layer_sizes_interleave():
+    """Kernel launch attributes are process-wide: contexts of different face
+    sizes must run interleaved (a small context configured last must not
+    break a larger one)."""
+    dh, c0 = 0.1, 343.0
+    dt = 0.5 * dh / (c0 * np.sqrt(3.0))
+    big = A.Simulation(A.build_scene([(0, 0, 0, 96, 64, 40)], [(10, 10, 10)], [(20, 20, 20)], dh, dt, c0, 5),
+                       max_steps=64)
+    small = A.Simulation(A.build_scene([(0, 0, 0, 16, 16, 16)], [(5, 5, 5)], [(8, 8, 8)], dh, dt, c0, 5),
+                         max_steps=64)
+    for sim in (big, small):
+        sim.set_source_series(0, np.hanning(64).astype(np.float32))
+    small.run(8)
+    big.run(8)
+    small.run(8)
+    big.run(40)
+    assert big.time_step == 48 and small.time_step == 16
+    assert np.isfinite(big.recorders()).all() and np.abs(big.recorders()).max() > 0
