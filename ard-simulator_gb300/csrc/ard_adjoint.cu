@@ -131,7 +131,7 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
           buf, ctx->d_dct, ctx->d_srcpts, (int)ctx->srcpts.size(), ctx->n_src_total, ab.gsrc, ctx->d_tb, tstep);
       ARD_CUDA(cudaGetLastError());
     }
-    if (int rc2 = launch_partial_sums<T>(ctx, s)) return rc2;
+    if (int rc2 = launch_post_modal<T>(ctx, s, 0, false)) return rc2;
     if (ctx->fused_faces) {
       face2d_kernel<T><<<grid_for((long long)ctx->adj2_2d.size(), 1, gx), kFace2DThreads, ctx->f2d_bytes, s>>>(
           buf, ctx->d_adj2_2d, (int)ctx->adj2_2d.size(), ctx->f2d_smem);

@@ -147,6 +147,7 @@ struct Face2DJob {
   long long tabA, tabB;
   int V, U, ld;
   int u0, ub;
+  int which;     // 0: both outputs; 1: out0 only; 2: out1 only (a pair split over two blocks)
   double scale;
 };
 

@@ -149,6 +149,7 @@ extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_o
   }
   ctx->num_sms = prop.multiProcessorCount;
   ctx->smem_optin = (int)prop.sharedMemPerBlockOptin;
+  ctx->smem_per_sm = prop.sharedMemPerMultiprocessor;
   int rc = build_layout(ctx.get(), scenes, n_scenes);
   if (rc == ARD_OK) rc = configure_kernels(ctx.get());
   if (rc) {
@@ -187,8 +188,7 @@ extern "C" int ard_kernels_per_step(const ard_ctx* c, int32_t* out) {
   if (!ctx->dct.empty()) {
     n += ctx->fused_faces ? 2 : 4;           // forward and inverse face transforms
     n += 1;                                  // modal update
-    n += ctx->recpts.empty() ? 0 : 1;        // recorder sums
-    n += ctx->psum.empty() ? 0 : 1;          // partial sums
+    n += (ctx->recpts.empty() && ctx->psum.empty()) ? 0 : 1;   // recorder sums + partial sums
   }
   n += ctx->n_face_cells > 0 ? 1 : 0;        // interfaces
   *out = n;
@@ -277,13 +277,8 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
       modal_kernel<T, false><<<mgrid, kModalThreads, msmem, s>>>(ma);
     ARD_CUDA(cudaGetLastError());
     ARD_CUDA(mark(kStageRecorder));
-    if (!ctx->recpts.empty()) {
-      recorder_kernel<T><<<grid_for((long long)ctx->recpts.size() * 32, 128, 1 << 30), 128, 0, s>>>(
-          buf, ctx->d_dct, ctx->d_recpts, (int)ctx->recpts.size(), ctx->d_hist, ctx->d_t, tstep, ctx->max_steps);
-      ARD_CUDA(cudaGetLastError());
-    }
+    if (int rc = launch_post_modal<T>(ctx, s, tstep, true)) return rc;
     ARD_CUDA(mark(kStageInvCols));
-    if (int rc = launch_partial_sums<T>(ctx, s)) return rc;
     if (ctx->fused_faces) {
       face2d_kernel<T><<<grid_for((long long)ctx->inv2d.size(), 1, gx), kFace2DThreads, ctx->f2d_bytes, s>>>(
           buf, ctx->d_inv2d, (int)ctx->inv2d.size(), ctx->f2d_smem);
@@ -314,17 +309,23 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   return ARD_OK;
 }
 
+// Recorder sums (with_recorders) and partial sums in one launch.
 template <typename T>
-int launch_partial_sums(Ctx* ctx, cudaStream_t s) {
-  if (ctx->psum.empty()) return ARD_OK;
-  partial_sum_kernel<T><<<grid_for(ctx->psum_total, 256, ctx->num_sms * 8), 256, 0, s>>>(
-      reinterpret_cast<T*>(ctx->d_buf), ctx->d_psum, (int)ctx->psum.size(), ctx->psum_total);
+int launch_post_modal(Ctx* ctx, cudaStream_t s, int tstep, bool with_recorders) {
+  const int nrec = with_recorders ? (int)ctx->recpts.size() : 0;
+  const int rec_blocks = (nrec * 32 + 255) / 256;
+  const int sum_blocks = ctx->psum.empty() ? 0 : grid_for(ctx->psum_total, 256, ctx->num_sms * 8);
+  if (rec_blocks + sum_blocks == 0) return ARD_OK;
+  PostModalArgs<T> a{reinterpret_cast<T*>(ctx->d_buf), ctx->d_dct, ctx->d_recpts, nrec, ctx->d_hist, ctx->d_t,
+                     tstep, ctx->max_steps, rec_blocks, ctx->d_psum, (int)ctx->psum.size(),
+                     ctx->psum.empty() ? 0 : ctx->psum_total};
+  post_modal_kernel<T><<<rec_blocks + sum_blocks, 256, 0, s>>>(a);
   ARD_CUDA(cudaGetLastError());
   return ARD_OK;
 }
 
-template int launch_partial_sums<float>(Ctx*, cudaStream_t);
-template int launch_partial_sums<double>(Ctx*, cudaStream_t);
+template int launch_post_modal<float>(Ctx*, cudaStream_t, int, bool);
+template int launch_post_modal<double>(Ctx*, cudaStream_t, int, bool);
 template int launch_step<float>(Ctx*, int, int, cudaStream_t, cudaStream_t, bool, cudaEvent_t*);
 template int launch_step<double>(Ctx*, int, int, cudaStream_t, cudaStream_t, bool, cudaEvent_t*);
 

@@ -39,6 +39,7 @@ struct Ctx {
   int device = 0;
   int num_sms = 1;
   int smem_optin = 48 * 1024;
+  size_t smem_per_sm = 228 * 1024;
   long long max_steps = 4096;
   bool use_graphs = true;
   bool debug_sync = false;          // ARD_DEBUG_SYNC=1: synchronise and check after every stage
@@ -122,7 +123,7 @@ int launch_steps_direct(Ctx* ctx, int n, cudaStream_t s);
 int ensure_graph(Ctx* ctx);
 int check_guards(Ctx* ctx);
 template <typename T>
-int launch_partial_sums(Ctx* ctx, cudaStream_t s);
+int launch_post_modal(Ctx* ctx, cudaStream_t s, int tstep, bool with_recorders);
 void build_adjoint_jobs(Ctx* ctx);
 void pml_profile_unit(const Ctx* ctx, int type, int L, std::vector<double>* out);
 template <typename T>

@@ -8,7 +8,8 @@
 //                       sources); M(t) = a (2 cos M(t-1) - M(t-2) + psi F);
 //                       contraction of M(t) onto the face rows and the
 //                       recorder cells
-//   recorder_kernel     recorder samples of step t
+//   post_modal_kernel   recorder samples of step t + sums of the contraction
+//                       partials
 //   xform_gemm_kernel   inverse 2D transforms -> pressure face layers
 //   pml_kernel          Grote-Sim PML update of every slab
 //   iface_kernel        6th-order interface forcing into the force face
@@ -208,17 +209,53 @@ struct SumJob {
   int nb;
 };
 
+// After the modal update: the recorder samples of the step (blocks
+// [0, rec_blocks): one warp per recorder, the sum of the tiles' partials
+// times s_i into the double history) and the in-place partial sums (the
+// other blocks, grid-stride).  One launch for both.
 template <typename T>
-__global__ void __launch_bounds__(256) partial_sum_kernel(T* __restrict__ buf, const SumJob* __restrict__ jobs,
-                                                           int njobs, long long total) {
-  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total;
-       g += (long long)gridDim.x * blockDim.x) {
-    int lo = 0, hi = njobs - 1;
+struct PostModalArgs {
+  T* buf;
+  const DctDev* dct;
+  const PointDev* recs;
+  int nrec_total;
+  double* hist;
+  const long long* tcount;
+  int tstep;
+  long long max_steps;
+  int rec_blocks;
+  const SumJob* jobs;
+  int njobs;
+  long long total;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
+  if ((int)blockIdx.x < a.rec_blocks) {
+    const int lane = threadIdx.x & 31;
+    const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (r >= a.nrec_total) return;
+    const PointDev q = a.recs[r];
+    const DctDev& D = a.dct[q.part];
+    const int local_r = r - D.rec0;
+    const int ntiles = D.nbx * D.nby * D.nbz;
+    T s = 0;
+    for (int i = lane; i < ntiles; i += 32) s += a.buf[D.recpart + (long long)i * D.nrec + local_r];
+    s = warp_sum(s);
+    const long long t = *a.tcount + a.tstep;
+    if (lane == 0 && t < a.max_steps) a.hist[t * a.nrec_total + q.slot] = (double)(s * (T)D.si);
+    return;
+  }
+  T* __restrict__ buf = a.buf;
+  const long long nb = (long long)gridDim.x - a.rec_blocks;
+  for (long long g = ((long long)blockIdx.x - a.rec_blocks) * blockDim.x + threadIdx.x; g < a.total;
+       g += nb * blockDim.x) {
+    int lo = 0, hi = a.njobs - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (jobs[mid].first <= g) lo = mid; else hi = mid - 1;
+      if (a.jobs[mid].first <= g) lo = mid; else hi = mid - 1;
     }
-    const SumJob J = jobs[lo];
+    const SumJob J = a.jobs[lo];
     const T* p = buf + J.base + (g - J.first);
     T v[4] = {0, 0, 0, 0};
     int b = 0;
@@ -308,30 +345,40 @@ __global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ 
     }
     __syncthreads();
     // ---- along U: T0 = E B, T1 = O B (lane = column, warp = row group) ----
-    for (int r0 = wrow; r0 < V; r0 += kRowStep) {
-      T e[4] = {0, 0, 0, 0}, o[4] = {0, 0, 0, 0};
-      int rr[4];
+    auto along_u = [&](auto de, auto dodd) {
+      constexpr bool DE = decltype(de)::value, DO = decltype(dodd)::value;
+      for (int r0 = wrow; r0 < V; r0 += kRowStep) {
+        T e[4] = {0, 0, 0, 0}, o[4] = {0, 0, 0, 0};
+        int rr[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) rr[i] = min(r0 + 8 * i, V - 1);
-      for (int j = 0; j < U; j += 4) {
-        const T b0 = Bs[j * 33 + lane], b1 = Bs[(j + 1) * 33 + lane];
-        const T b2 = Bs[(j + 2) * 33 + lane], b3 = Bs[(j + 3) * 33 + lane];
+        for (int i = 0; i < 4; ++i) rr[i] = min(r0 + 8 * i, V - 1);
+        for (int j = 0; j < U; j += 4) {
+          const T b0 = Bs[j * 33 + lane], b1 = Bs[(j + 1) * 33 + lane];
+          const T b2 = Bs[(j + 2) * 33 + lane], b3 = Bs[(j + 3) * 33 + lane];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          T x[4], y[4];
-          load4(X0 + rr[i] * xp + j, x);
-          load4(X1 + rr[i] * xp + j, y);
-          e[i] += x[0] * b0 + x[1] * b1 + x[2] * b2 + x[3] * b3;
-          o[i] += y[0] * b0 + y[1] * b1 + y[2] * b2 + y[3] * b3;
+          for (int i = 0; i < 4; ++i) {
+            T x[4], y[4];
+            if constexpr (DE) {
+              load4(X0 + rr[i] * xp + j, x);
+              e[i] += x[0] * b0 + x[1] * b1 + x[2] * b2 + x[3] * b3;
+            }
+            if constexpr (DO) {
+              load4(X1 + rr[i] * xp + j, y);
+              o[i] += y[0] * b0 + y[1] * b1 + y[2] * b2 + y[3] * b3;
+            }
+          }
         }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (r0 + 8 * i < V) {
+            if constexpr (DE) T0[(r0 + 8 * i) * 33 + lane] = e[i];
+            if constexpr (DO) T1[(r0 + 8 * i) * 33 + lane] = o[i];
+          }
       }
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-        if (r0 + 8 * i < V) {
-          T0[(r0 + 8 * i) * 33 + lane] = e[i];
-          T1[(r0 + 8 * i) * 33 + lane] = o[i];
-        }
-    }
+    };
+    if (J.which == 0) along_u(std::true_type{}, std::true_type{});
+    else if (J.which == 1) along_u(std::true_type{}, std::false_type{});
+    else along_u(std::false_type{}, std::true_type{});
     __syncthreads();
     // ---- A (V x V, row o contiguous) into the X0 area (asynchronous) ----
     const T* A = buf + J.tabA;
@@ -354,37 +401,43 @@ __global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ 
     __syncthreads();
     // ---- along V: out = scale A T ----
     const T scale = (T)J.scale;
-    for (int o0 = wrow; o0 < V; o0 += kRowStep) {
-      T e[4] = {0, 0, 0, 0}, od[4] = {0, 0, 0, 0};
-      int oo[4];
+    auto along_v = [&](auto de, auto dodd) {
+      constexpr bool DE = decltype(de)::value, DO = decltype(dodd)::value;
+      for (int o0 = wrow; o0 < V; o0 += kRowStep) {
+        T e[4] = {0, 0, 0, 0}, od[4] = {0, 0, 0, 0};
+        int oo[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) oo[i] = min(o0 + 8 * i, V - 1);
-      for (int r = 0; r < V; r += 4) {
-        T t[4], u[4];
+        for (int i = 0; i < 4; ++i) oo[i] = min(o0 + 8 * i, V - 1);
+        for (int r = 0; r < V; r += 4) {
+          T t[4], u[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const bool ok = r + k < V;
-          t[k] = ok ? T0[(r + k) * 33 + lane] : (T)0;
-          u[k] = ok ? T1[(r + k) * 33 + lane] : (T)0;
-        }
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          T a4[4];
-          load4(X0 + oo[i] * ap + r, a4);
-          e[i] += a4[0] * t[0] + a4[1] * t[1] + a4[2] * t[2] + a4[3] * t[3];
-          od[i] += a4[0] * u[0] + a4[1] * u[1] + a4[2] * u[2] + a4[3] * u[3];
-        }
-      }
-      if (lane < J.ub) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-          if (o0 + 8 * i < V) {
-            const long long off = (long long)(o0 + 8 * i) * J.ld + J.u0 + lane;
-            buf[J.out0 + off] = e[i] * scale;
-            buf[J.out1 + off] = od[i] * scale;
+          for (int k = 0; k < 4; ++k) {
+            const bool ok = r + k < V;
+            if constexpr (DE) t[k] = ok ? T0[(r + k) * 33 + lane] : (T)0;
+            if constexpr (DO) u[k] = ok ? T1[(r + k) * 33 + lane] : (T)0;
           }
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            T a4[4];
+            load4(X0 + oo[i] * ap + r, a4);
+            if constexpr (DE) e[i] += a4[0] * t[0] + a4[1] * t[1] + a4[2] * t[2] + a4[3] * t[3];
+            if constexpr (DO) od[i] += a4[0] * u[0] + a4[1] * u[1] + a4[2] * u[2] + a4[3] * u[3];
+          }
+        }
+        if (lane < J.ub) {
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if (o0 + 8 * i < V) {
+              const long long off = (long long)(o0 + 8 * i) * J.ld + J.u0 + lane;
+              if constexpr (DE) buf[J.out0 + off] = e[i] * scale;
+              if constexpr (DO) buf[J.out1 + off] = od[i] * scale;
+            }
+        }
       }
-    }
+    };
+    if (J.which == 0) along_v(std::true_type{}, std::true_type{});
+    else if (J.which == 1) along_v(std::true_type{}, std::false_type{});
+    else along_v(std::false_type{}, std::true_type{});
   }
 }
 
@@ -761,24 +814,6 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
   }
 }
 
-// Recorder samples of the current step: sum of the modal tiles' partials.
-template <typename T>
-__global__ void recorder_kernel(const T* __restrict__ buf, const DctDev* __restrict__ dct, const PointDev* __restrict__ recs,
-                                int nrec_total, double* __restrict__ hist, const long long* tcount, int tstep,
-                                long long max_steps) {
-  const int lane = threadIdx.x & 31;
-  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (r >= nrec_total) return;
-  const PointDev q = recs[r];
-  const DctDev& D = dct[q.part];
-  const int local_r = r - D.rec0;
-  const int ntiles = D.nbx * D.nby * D.nbz;
-  T s = 0;
-  for (int i = lane; i < ntiles; i += 32) s += buf[D.recpart + (long long)i * D.nrec + local_r];
-  s = warp_sum(s);
-  const long long t = *tcount + tstep;
-  if (lane == 0 && t < max_steps) hist[t * nrec_total + q.slot] = (double)(s * (T)D.si);
-}
 
 // ---------------------------------------------------------------------------
 // PML

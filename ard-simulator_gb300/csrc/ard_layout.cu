@@ -142,6 +142,26 @@ int zero_state(Ctx* ctx) {
   return ARD_OK;
 }
 
+// Splits the largest two-output face jobs into one-output jobs (the same
+// staging, half the arithmetic) while the list still fits in one wave of
+// `slots` blocks: the launch lasts as long as its largest job.  Largest
+// first afterwards.
+void balance_face_jobs(std::vector<Face2DJob>* jobs, int slots) {
+  auto work = [](const Face2DJob& j) { return (long long)j.V * (j.U + j.V) * (j.which == 0 ? 2 : 1); };
+  while ((int)jobs->size() < slots && !jobs->empty()) {
+    size_t k = 0;
+    for (size_t i = 1; i < jobs->size(); ++i)
+      if (work((*jobs)[i]) > work((*jobs)[k])) k = i;
+    if ((*jobs)[k].which != 0) break;   // the largest is already single: splitting others cannot help
+    Face2DJob b = (*jobs)[k];
+    (*jobs)[k].which = 1;
+    b.which = 2;
+    jobs->push_back(b);
+  }
+  std::stable_sort(jobs->begin(), jobs->end(),
+                   [&](const Face2DJob& a, const Face2DJob& b) { return work(a) > work(b); });
+}
+
 // Face transforms of the adjoint step, the transposes of the forward ones:
 //   adjoint of the inverse transform: Q[pm][n] = s_i Ci_V (q_n +/- q_{5-n}) Ci_U^T
 //     (the adjoint face pressure q -> the P arrays read by the adjoint modal step)
@@ -198,7 +218,7 @@ void build_adjoint_jobs(Ctx* ctx) {
         const int n = L < 3 ? L : 5 - L;
         XformJob j{};     // columns along V with C_V^T: A(o, r) = C_V[r][o]
         j.in0 = a.R + (0 * 3 + n) * LS; j.in1 = a.R + (1 * 3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
-        j.nparts = 1; j.part_stride = 0;   // partials summed beforehand (partial_sum_kernel)
+        j.nparts = 1; j.part_stride = 0;   // partials summed beforehand (post_modal_kernel)
         j.out = a.tmp + L * LS; j.ctab = a.cV; j.n = a.V; j.batch = a.U; j.ld = a.ld;
         j.inverse = 1; j.rows = 0; j.scale = 1.0;
         add_job(ctx->adjg[2], j);
@@ -621,7 +641,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         const int n = L < 3 ? L : 5 - L;
         XformJob j{};
         j.in0 = a.R + (0 * 3 + n) * LS; j.in1 = a.R + (1 * 3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
-        j.nparts = 1; j.part_stride = 0;   // partials summed beforehand (partial_sum_kernel)
+        j.nparts = 1; j.part_stride = 0;   // partials summed beforehand (post_modal_kernel)
         j.out = a.tmp + L * LS; j.ctab = a.cV + (long long)a.nV * a.nV; j.n = a.nV; j.batch = a.nU; j.ld = a.ld;
         j.inverse = 1; j.rows = 0; j.scale = 1.0;
         add_job(ctx->inv1, j);
@@ -677,6 +697,14 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     ctx->fused_faces = !ctx->dct.empty() && ctx->f2d_bytes <= (size_t)std::min(ctx->smem_optin, 200 * 1024);
   }
   if (ctx->adjoint) build_adjoint_jobs(ctx);
+  if (ctx->fused_faces) {
+    const int per_sm = std::max(1, (int)(ctx->smem_per_sm / (ctx->f2d_bytes + 1024)));
+    const int slots = ctx->num_sms * per_sm;
+    balance_face_jobs(&ctx->fwd2d, slots);
+    balance_face_jobs(&ctx->inv2d, slots);
+    balance_face_jobs(&ctx->adj1_2d, slots);
+    balance_face_jobs(&ctx->adj2_2d, slots);
+  }
 
   // ---- device allocation ----
   const size_t es = elem_size(ctx);

@@ -255,7 +255,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=None, help="steps of the adjoint measurement (default: sim steps)")
-    ap.add_argument("--checkpoint-every", type=int, default=64)
+    ap.add_argument("--checkpoint-every", type=int, default=0,
+                    help="adjoint checkpoint interval (0: keep the whole PML history when it fits, else automatic)")
     ap.add_argument("--plain", action="store_true", help="one context per scene, run one after another")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -406,10 +407,12 @@ def main():
     alg_bytes = BYTES_PER_AIR_CELL * n_air
     achieved = alg_bytes / (modal_ms / 1e3) / 1e9 if modal_ms > 0 else 0.0
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"traffic_{args.config}.json")
+    tpath = os.path.join(ROOT, "profiles", f"traffic_{args.config}.txt")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get("modal_kernel_dram_bytes_per_launch")
+            for ln in f:
+                if ln.startswith("modal_kernel_dram_bytes_per_launch:"):
+                    traffic = int(ln.split(":")[1])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "kernel": "modal_kernel<float>", "algorithmic_bytes_per_launch": alg_bytes,
