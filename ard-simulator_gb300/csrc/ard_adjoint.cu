@@ -156,15 +156,72 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
   return ARD_OK;
 }
 
-// Adjoint steps t_hi - 1 down to t_lo.
+static __global__ void retreat_counter_kernel(long long* tc, int n) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) tc[0] -= n;
+}
+
+// Adjoint steps captured as one CUDA graph: kAdjGraphSteps steps starting at
+// a step t = 5 (mod 6) (the level choices t % 3 and t & 1 repeat every 6
+// steps), the step counter lowered by kAdjGraphSteps at the end.
+constexpr int kAdjGraphSteps = 48;
+
+struct AdjGraph {
+  cudaGraphExec_t exec = nullptr;
+  ~AdjGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+template <typename T>
+int capture_adjoint_graph(Ctx* ctx, const AdjBuffers& ab, const HistView& hv, AdjGraph* g) {
+  if (g->exec) return ARD_OK;
+  cudaGraph_t graph = nullptr;
+  ARD_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  const int t_pattern = 6 * 1000 + 5;
+  int rc = ARD_OK;
+  for (int i = 0; i < kAdjGraphSteps && rc == ARD_OK; ++i)
+    rc = launch_adjoint_step<T>(ctx, t_pattern - i, i, ctx->stream, ctx->stream2, ab, hv);
+  if (rc == ARD_OK) retreat_counter_kernel<<<1, 32, 0, ctx->stream>>>(ctx->d_tb, kAdjGraphSteps);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+  if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+  if (e != cudaSuccess) { ctx->err = std::string("adjoint graph capture: ") + cudaGetErrorString(e); return ARD_ERR_CUDA; }
+  e = cudaGraphInstantiate(&g->exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) { ctx->err = std::string("adjoint graph instantiate: ") + cudaGetErrorString(e); return ARD_ERR_CUDA; }
+  return ARD_OK;
+}
+
+// Adjoint steps t_hi - 1 down to t_lo: direct launches up to a step t = 5
+// (mod 6), then 48-step graphs, then direct launches for the rest.  Every
+// launch finds its step as counter - tstep.
 template <typename T>
 int run_backward(Ctx* ctx, long long t_hi, long long t_lo, long long hist_t0, const AdjBuffers& ab,
-                 const HistView& hv) {
+                 const HistView& hv, AdjGraph* graph) {
   cudaStream_t s = ctx->stream;
-  set_counters_kernel<<<1, 32, 0, s>>>(ctx->d_tb, t_hi - 1, hist_t0);
+  long long t = t_hi - 1;
+  long long base = t;
+  set_counters_kernel<<<1, 32, 0, s>>>(ctx->d_tb, base, hist_t0);
   ARD_CUDA(cudaGetLastError());
-  for (long long t = t_hi - 1; t >= t_lo; --t) {
-    int rc = launch_adjoint_step<T>(ctx, (int)t, (int)(t_hi - 1 - t), s, ctx->stream2, ab, hv);
+  const bool graphs = ctx->use_graphs && !ctx->debug_sync;
+  while (t >= t_lo) {
+    if (graphs && t % 6 == 5 && t - t_lo + 1 >= kAdjGraphSteps) break;
+    int rc = launch_adjoint_step<T>(ctx, (int)t, (int)(base - t), s, ctx->stream2, ab, hv);
+    if (rc) return rc;
+    --t;
+  }
+  if (graphs && t >= t_lo && t - t_lo + 1 >= kAdjGraphSteps) {
+    int rc = capture_adjoint_graph<T>(ctx, ab, hv, graph);
+    if (rc) return rc;
+    set_counters_kernel<<<1, 32, 0, s>>>(ctx->d_tb, t, hist_t0);
+    ARD_CUDA(cudaGetLastError());
+    while (t - t_lo + 1 >= kAdjGraphSteps) {
+      ARD_CUDA(cudaGraphLaunch(graph->exec, s));
+      t -= kAdjGraphSteps;
+    }
+    base = t;   // the counter now holds t
+  }
+  for (; t >= t_lo; --t) {
+    int rc = launch_adjoint_step<T>(ctx, (int)t, (int)(base - t), s, ctx->stream2, ab, hv);
     if (rc) return rc;
   }
   return ARD_OK;
@@ -282,6 +339,7 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
   const long long adj_len = ctx->adj_end - ctx->adj_begin;
   ARD_CUDA(cudaMemsetAsync(buf + ctx->adj_begin, 0, adj_len * es, s));
   const HistView hv = need_hist ? HistView{ab.hist_p, ab.hist_phn, hlen, ab.gz} : HistView{};
+  AdjGraph graph;   // captured on first use, for this call's buffers
   if (use_ckpt) {
     for (long long i = n_ckpt - 1; i >= 0; --i) {
       const long long t0 = i * K, t1 = std::min(T_steps, t0 + K);
@@ -294,7 +352,7 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
       rc = ard_step(handle, t1 - t0, nullptr);
       if (rc) return rc;
       if ((rc = stop_history())) return rc;
-      rc = run_backward<T>(ctx, t1, t0, t0, ab, hv);
+      rc = run_backward<T>(ctx, t1, t0, t0, ab, hv, &graph);
       if (rc) return rc;
     }
     // leave the forward state as after step T
@@ -303,7 +361,7 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
     ARD_CUDA(cudaGetLastError());
     ctx->t_host = T_steps;
   } else {
-    rc = run_backward<T>(ctx, T_steps, 0, 0, ab, hv);
+    rc = run_backward<T>(ctx, T_steps, 0, 0, ab, hv, &graph);
     if (rc) return rc;
   }
   ARD_CUDA(cudaStreamSynchronize(s));

@@ -157,7 +157,7 @@ struct PmlAdjArgs {
 //   dJ/dz(l) += sum over layer l of  -dt X (p(t) - p(t-1))
 //               - dt Phi_n (phi_n(t) + Dn p(t)) + dt Phi_a Da p(t) + dt Phi_b Db p(t)
 template <typename T>
-__global__ void __launch_bounds__(256) pml_adjoint_kernel(PmlAdjArgs<T> a) {
+__global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
   constexpr int TA = 8, TB = 32;
   __shared__ T Xs[TA + 6][TB + 6];
   __shared__ T FA[TA + 4][TB];
@@ -175,6 +175,7 @@ __global__ void __launch_bounds__(256) pml_adjoint_kernel(PmlAdjArgs<T> a) {
     hofs = t - a.tc[1];   // hist_p[hofs + 1] = p(t), hist_p[hofs] = p(t-1), hist_phn[hofs] = phi_n(t)
   }
   const T dt = a.dt, dt2 = a.dt * a.dt;
+  const T r180 = (T)1 / ((T)180 * a.dh * a.dh), r12 = (T)1 / ((T)12 * a.dh);
   for (int bi = blockIdx.x; bi < a.nblocks; bi += gridDim.x) {
     const int4 blk = a.blocks[bi];
     const PmlDev& P = a.pml[blk.x];
@@ -211,39 +212,75 @@ __global__ void __launch_bounds__(256) pml_adjoint_kernel(PmlAdjArgs<T> a) {
       zw[m] = ok ? zeta[ll] * Fn[ll * lstride + col] : (T)0;
       qw[m] = (ok && zgrad) ? hp[ll * lstride + col] : (T)0;
     }
-    T gacc[kMaxPmlLayers];
-#pragma unroll
-    for (int q = 0; q < kMaxPmlLayers; ++q) gacc[q] = 0;
-    const T d180 = (T)180 * a.dh * a.dh, d12 = (T)12 * a.dh;
-    for (int l = 0; l < L; ++l) {
+    __syncthreads();  // the previous tile's layer sums have been read
+    if (threadIdx.x < 8 * kMaxPmlLayers) red[threadIdx.x / kMaxPmlLayers][threadIdx.x % kMaxPmlLayers] = 0;
+    // the next layer's tiles and point values, fetched while the current layer computes
+    T nX[3], nA[2], nB[2], nQ[2], ny = 0, no = 0, nfn = 0, npp = 0, nhf = 0;
+    auto fetch = [&](int l) {
       const T* Xl = X + l * lstride;
       const T* fal = Fa + l * lstride;
       const T* fbl = Fb + l * lstride;
-      __syncthreads();  // previous layer done with the tiles
-      for (int i = threadIdx.x; i < (TA + 6) * (TB + 6); i += 256) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int i = threadIdx.x + 256 * k;
         const int r = i / (TB + 6), c = i - r * (TB + 6);
         const int aa = a0 + r - 3, bb = b0 + c - 3;
-        Xs[r][c] = (aa >= 0 && aa < A && bb >= 0 && bb < B) ? Xl[(long long)aa * B + bb] : (T)0;
+        nX[k] = (i < (TA + 6) * (TB + 6) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? Xl[(long long)aa * B + bb] : (T)0;
       }
-      for (int i = threadIdx.x; i < (TA + 4) * TB; i += 256) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int i = threadIdx.x + 256 * k;
         const int r = i / TB, c = i - r * TB;
         const int aa = a0 + r - 2, bb = b0 + c;
-        FA[r][c] = (aa >= 0 && aa < A && bb < B) ? fal[(long long)aa * B + bb] : (T)0;
+        nA[k] = (i < (TA + 4) * TB && aa >= 0 && aa < A && bb < B) ? fal[(long long)aa * B + bb] : (T)0;
       }
-      for (int i = threadIdx.x; i < TA * (TB + 4); i += 256) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int i = threadIdx.x + 256 * k;
         const int r = i / (TB + 4), c = i - r * (TB + 4);
         const int aa = a0 + r, bb = b0 + c - 2;
-        FB[r][c] = (aa < A && bb >= 0 && bb < B) ? fbl[(long long)aa * B + bb] : (T)0;
+        nB[k] = (i < TA * (TB + 4) && aa < A && bb >= 0 && bb < B) ? fbl[(long long)aa * B + bb] : (T)0;
       }
+      const long long I = l * lstride + col;
+      ny = inside ? Y[I] : (T)0;
+      no = inside ? O[I] : (T)0;
+      nfn = inside ? Fn[I] : (T)0;
       if (zgrad) {
         const T* hpl = hp + l * lstride;
-        for (int i = threadIdx.x; i < (TA + 4) * (TB + 4); i += 256) {
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          const int i = threadIdx.x + 256 * k;
           const int r = i / (TB + 4), c = i - r * (TB + 4);
           const int aa = a0 + r - 2, bb = b0 + c - 2;
-          Qs[r][c] = (aa >= 0 && aa < A && bb >= 0 && bb < B) ? hpl[(long long)aa * B + bb] : (T)0;
+          nQ[k] = (i < (TA + 4) * (TB + 4) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? hpl[(long long)aa * B + bb]
+                                                                                        : (T)0;
         }
+        npp = inside ? hpp[I] : (T)0;
+        nhf = inside ? hfn[I] : (T)0;
       }
+    };
+    auto commit = [&]() {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int i = threadIdx.x + 256 * k;
+        if (i < (TA + 6) * (TB + 6)) Xs[i / (TB + 6)][i % (TB + 6)] = nX[k];
+      }
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int i = threadIdx.x + 256 * k;
+        if (i < (TA + 4) * TB) FA[i / TB][i % TB] = nA[k];
+        if (i < TA * (TB + 4)) FB[i / (TB + 4)][i % (TB + 4)] = nB[k];
+        if (zgrad && i < (TA + 4) * (TB + 4)) Qs[i / (TB + 4)][i % (TB + 4)] = nQ[k];
+      }
+    };
+    fetch(0);
+    for (int l = 0; l < L; ++l) {
+      __syncthreads();  // previous layer done with the tiles
+      commit();
+      const T y0 = ny, o0 = no, fn0 = nfn, pp0 = npp, hf0 = nhf;
+      if (l + 1 < L) fetch(l + 1);
       __syncthreads();
+      T g = 0;
       if (inside) {
         T lx = 0;
 #pragma unroll
@@ -258,14 +295,14 @@ __global__ void __launch_bounds__(256) pml_adjoint_kernel(PmlAdjArgs<T> a) {
           daf += c5[m] * FA[ta + m][tb];
           dbf += c5[m] * FB[ta][tb + m];
         }
-        lx /= d180;
-        dnx /= d12; dax /= d12; dbx /= d12;
-        dnz /= d12; daf /= d12; dbf /= d12;
+        lx *= r180;
+        dnx *= r12; dax *= r12; dbx *= r12;
+        dnz *= r12; daf *= r12; dbf *= r12;
         const long long I = l * lstride + col;
         const T zn = zeta[l];
-        const T x0 = xw[3], y0 = Y[I];
-        const T fn0 = Fn[I], fa0 = FA[ta + 2][tb], fb0 = FB[ta][tb + 2];
-        O[I] = O[I] + (T)2 * x0 + dt2 * a.c0 * a.c0 * lx - dt * zn * x0 + (dt * zn - (T)1) * y0 + dt * dnz -
+        const T x0 = xw[3];
+        const T fa0 = FA[ta + 2][tb], fb0 = FB[ta][tb + 2];
+        O[I] = o0 + (T)2 * x0 + dt2 * a.c0 * a.c0 * lx - dt * zn * x0 + (dt * zn - (T)1) * y0 + dt * dnz -
                dt * zn * (daf + dbf);
         Y[I] = 0;
         Fn_o[I] = ((T)1 - dt * zn) * fn0 - dt2 * dnx;
@@ -279,12 +316,13 @@ __global__ void __launch_bounds__(256) pml_adjoint_kernel(PmlAdjArgs<T> a) {
             dap += c5[m] * Qs[ta + m][tb + 2];
             dbp += c5[m] * Qs[ta + 2][tb + m];
           }
-          dnp /= d12; dap /= d12; dbp /= d12;
-          const T g = -dt * x0 * (qw[2] - hpp[I]) - dt * fn0 * (hfn[I] + dnp) + dt * (fa0 * dap + fb0 * dbp);
-#pragma unroll
-          for (int q = 0; q < kMaxPmlLayers; ++q)
-            if (q == l) gacc[q] += g;
+          dnp *= r12; dap *= r12; dbp *= r12;
+          g = -dt * x0 * (qw[2] - pp0) - dt * fn0 * (hf0 + dnp) + dt * (fa0 * dap + fb0 * dbp);
         }
+      }
+      if (zgrad) {
+        const double sw = warp_sum((double)g);
+        if (lane == 0) red[warp][l] += sw;
       }
       // slide the windows one layer
 #pragma unroll
@@ -297,16 +335,11 @@ __global__ void __launch_bounds__(256) pml_adjoint_kernel(PmlAdjArgs<T> a) {
       qw[4] = (ok3 && zgrad) ? hp[(l + 3) * lstride + col] : (T)0;
     }
     if (zgrad) {
-#pragma unroll
-      for (int q = 0; q < kMaxPmlLayers; ++q) {
-        const double s = warp_sum((double)gacc[q]);
-        if (lane == 0) red[warp][q] = s;
-      }
       __syncthreads();
       if (threadIdx.x < L) {
-        double s = 0;
-        for (int w8 = 0; w8 < 8; ++w8) s += red[w8][threadIdx.x];
-        a.gz[(long long)bi * kMaxPmlLayers + threadIdx.x] += s;
+        double sum = 0;
+        for (int w8 = 0; w8 < 8; ++w8) sum += red[w8][threadIdx.x];
+        a.gz[(long long)bi * kMaxPmlLayers + threadIdx.x] += sum;
       }
     }
   }
