@@ -106,6 +106,7 @@ SIGNATURES = {
                               C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "ard_read_initial_pressure_grad": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
     "ard_kernels_per_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "ard_describe": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     "ard_profile_steps": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "ard_last_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
 }
@@ -263,13 +264,14 @@ class Simulation:
     """Context over one or many scenes (many = batched mode)."""
 
     def __init__(self, scenes, precision=PREC_F32, max_steps=4096, use_graphs=True, device=0,
-                 arithmetic=ARITH_ACCURATE, adjoint=False):
+                 arithmetic=ARITH_ACCURATE, adjoint=False, autotune=False):
         if isinstance(scenes, Scene):
             scenes = [scenes]
         self.scenes = list(scenes)
         arr = (SceneDesc * len(self.scenes))(*[s.desc for s in self.scenes])
         self._arr = arr
-        opt = Options(precision, max_steps, 1 if use_graphs else 0, device, 0, arithmetic, 1 if adjoint else 0)
+        opt = Options(precision, max_steps, 1 if use_graphs else 0, device, 1 if autotune else 0, arithmetic,
+                      1 if adjoint else 0)
         h = C.c_void_p()
         _check(lib().ard_create(arr, len(self.scenes), C.byref(opt), C.byref(h)))
         self._h = h
@@ -324,6 +326,13 @@ class Simulation:
 
     def synchronize(self):
         self._c(lib().ard_synchronize(self._h))
+
+    @property
+    def layout(self):
+        """The layout choices of the context (ard_describe)."""
+        b = C.create_string_buffer(4096)
+        self._c(lib().ard_describe(self._h, b, 4096))
+        return b.value.decode()
 
     @property
     def kernels_per_step(self):

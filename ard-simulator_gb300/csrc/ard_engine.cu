@@ -150,14 +150,95 @@ extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_o
   ctx->num_sms = prop.multiProcessorCount;
   ctx->smem_optin = (int)prop.sharedMemPerBlockOptin;
   ctx->smem_per_sm = prop.sharedMemPerMultiprocessor;
-  int rc = build_layout(ctx.get(), scenes, n_scenes);
-  if (rc == ARD_OK) rc = configure_kernels(ctx.get());
+  const bool autotune = opt && opt->autotune != 0;
+  auto describe = [](const Ctx* c) {
+    return std::string("tiles x") + std::to_string(c->tune_tiles) + ", lanes/row " +
+           (c->tune_g_shift ? "narrow" : "fit") + ", faces " + (c->fused_faces ? "fused" : "gemm") + ", " +
+           std::to_string(c->tiles.size()) + " modal tiles";
+  };
+  if (!autotune) {
+    int rc = build_layout(ctx.get(), scenes, n_scenes);
+    if (rc == ARD_OK) rc = configure_kernels(ctx.get());
+    if (rc) {
+      g_create_error = ctx->err;
+      free_ctx_device(ctx.get());
+      return rc;
+    }
+    ctx->tuning = describe(ctx.get());
+    *out = reinterpret_cast<ard_ctx*>(ctx.release());
+    return ARD_OK;
+  }
+  // Autotuner: build the context for each candidate layout, time real steps
+  // (CUDA graphs, the production path), keep the fastest.
+  struct Cand { int tiles, gshift, gemm; };
+  const Cand cands[] = {{1, 0, 0}, {2, 0, 0}, {4, 0, 0}, {1, 1, 0}, {2, 1, 0}, {1, 0, 1}};
+  std::unique_ptr<Ctx> best;
+  float best_ms = 0.f;
+  std::string report;
+  const int warm = 64, timed = 64;
+  for (const Cand& cd : cands) {
+    auto c = std::make_unique<Ctx>();
+    c->prec = ctx->prec; c->max_steps = std::max<long long>(ctx->max_steps, warm + timed);
+    c->use_graphs = ctx->use_graphs; c->device = ctx->device; c->arith = ctx->arith; c->adjoint = ctx->adjoint;
+    c->debug_sync = ctx->debug_sync; c->num_sms = ctx->num_sms; c->smem_optin = ctx->smem_optin;
+    c->smem_per_sm = ctx->smem_per_sm;
+    c->tune_tiles = cd.tiles; c->tune_g_shift = cd.gshift; c->tune_gemm = cd.gemm;
+    int rc = build_layout(c.get(), scenes, n_scenes);
+    if (rc == ARD_OK) rc = configure_kernels(c.get());
+    // the GEMM candidate is a distinct layout only where the fused transforms fit
+    if (rc == ARD_OK && cd.gemm &&
+        (c->dct.empty() || c->f2d_bytes > (size_t)std::min(c->smem_optin, 200 * 1024)))
+      rc = ARD_ERR_INVALID;
+    float ms = 0.f;
+    if (rc == ARD_OK) {
+      ard_ctx* h = reinterpret_cast<ard_ctx*>(c.get());
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      rc = ard_step(h, warm, nullptr);
+      if (rc == ARD_OK && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+        cudaEventRecord(e0, c->stream);
+        rc = ard_step(h, timed, nullptr);
+        cudaEventRecord(e1, c->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = ARD_ERR_CUDA;
+      }
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+    }
+    if (rc != ARD_OK) {
+      free_ctx_device(c.get());
+      continue;
+    }
+    report += "[" + describe(c.get()) + ": " + std::to_string(ms / timed * 1000.f) + " us/step] ";
+    if (!best || ms < best_ms) {
+      if (best) free_ctx_device(best.get());
+      best = std::move(c);
+      best_ms = ms;
+    } else {
+      free_ctx_device(c.get());
+    }
+  }
+  if (!best) {
+    g_create_error = "ard_create: no autotuner candidate could be built";
+    return ARD_ERR_INVALID;
+  }
+  best->max_steps = ctx->max_steps < best->max_steps ? best->max_steps : ctx->max_steps;
+  int rc = ard_reset(reinterpret_cast<ard_ctx*>(best.get()));
+  if (rc == ARD_OK) rc = configure_kernels(best.get());   // attributes of the kept layout last
   if (rc) {
-    g_create_error = ctx->err;
-    free_ctx_device(ctx.get());
+    g_create_error = best->err;
+    free_ctx_device(best.get());
     return rc;
   }
-  *out = reinterpret_cast<ard_ctx*>(ctx.release());
+  best->tuning = "autotuned: " + describe(best.get()) + "; candidates " + report;
+  *out = reinterpret_cast<ard_ctx*>(best.release());
+  return ARD_OK;
+}
+
+extern "C" int ard_describe(const ard_ctx* c, char* buf, int64_t n) {
+  if (!c || !buf || n < 1) return ARD_ERR_INVALID;
+  const std::string& e = reinterpret_cast<const Ctx*>(c)->tuning;
+  const size_t k = std::min<size_t>((size_t)(n - 1), e.size());
+  std::memcpy(buf, e.data(), k);
+  buf[k] = 0;
   return ARD_OK;
 }
 

@@ -75,6 +75,11 @@ struct Ctx {
   long long adj_begin = 0, adj_end = 0;      // adjoint state block
   long long pml_region[8][2] = {};           // all slabs' p0, p1, phn0, phn1, pha0, pha1, phb0, phb1
   bool adjoint = false;
+  // layout choices (the autotuner varies them; defaults are the heuristics)
+  int tune_tiles = 1;      // modal tiles per wave slot (x 2 per SM): kz split finer when > 1
+  int tune_g_shift = 0;    // 1: ky rows one lane-size narrower (more kx tiles, more ky rows per tile)
+  int tune_gemm = 0;       // 1: two-pass GEMM face transforms even when the fused ones fit
+  std::string tuning;      // description of the chosen layout
   // adjoint face transforms (options.adjoint): fused 2D jobs and the two-pass
   // GEMM form (q rows, q columns, R columns, R rows)
   std::vector<Face2DJob> adj1_2d, adj2_2d;

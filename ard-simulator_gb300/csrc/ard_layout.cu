@@ -359,6 +359,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   for (DctDev& D : ctx->dct) {
     const int need = std::min(D.wp, 128) / 4;
     D.G = need <= 8 ? 8 : (need <= 16 ? 16 : 32);
+    if (ctx->tune_g_shift && D.G > 8) D.G /= 2;
     D.kxt = 4 * D.G;
     D.rpc = kModalThreads / D.G;
     D.nbx = (D.wp + D.kxt - 1) / D.kxt;
@@ -366,7 +367,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     col_tiles += (long long)D.nbx * D.nby;
   }
   // resident slots: 2 tiles per SM; split kz only while the tiles still fit one wave
-  const long long slots = (long long)ctx->num_sms * 2;
+  const long long slots = (long long)ctx->num_sms * 2 * std::max(1, ctx->tune_tiles);
   for (size_t k = 0; k < ctx->dct.size(); ++k) {
     DctDev& D = ctx->dct[k];
     long long nbz = col_tiles > 0 ? slots / col_tiles : 1;
@@ -694,7 +695,8 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     }
     ctx->f2d_smem = Face2DSmem{(int)xs, (int)x1, (int)bs, (int)ts};
     ctx->f2d_bytes = (size_t)(xs + x1 + bs + 2 * ts) * es0;
-    ctx->fused_faces = !ctx->dct.empty() && ctx->f2d_bytes <= (size_t)std::min(ctx->smem_optin, 200 * 1024);
+    ctx->fused_faces = !ctx->dct.empty() && !ctx->tune_gemm &&
+                       ctx->f2d_bytes <= (size_t)std::min(ctx->smem_optin, 200 * 1024);
   }
   if (ctx->adjoint) build_adjoint_jobs(ctx);
   if (ctx->fused_faces) {

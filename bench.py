@@ -258,6 +258,7 @@ def main():
     ap.add_argument("--checkpoint-every", type=int, default=0,
                     help="adjoint checkpoint interval (0: keep the whole PML history when it fits, else automatic)")
     ap.add_argument("--plain", action="store_true", help="one context per scene, run one after another")
+    ap.add_argument("--autotune", action="store_true", help="let ard_create time candidate layouts and keep the fastest")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
@@ -285,8 +286,8 @@ def main():
     n_pml = sum(s.pml_cells for s in scenes)
     n_src = sum(len(sc["sources"]) for sc in cfg["scenes"])
     n_rec = sum(len(sc["recorders"]) for sc in cfg["scenes"])
-    sims = [A.Simulation([sc], max_steps=S, device=local) for sc in scenes] if args.plain else None
-    sim = sims[0] if args.plain else A.Simulation(scenes, max_steps=S, device=local)
+    sims = [A.Simulation([sc], max_steps=S, device=local, autotune=args.autotune) for sc in scenes] if args.plain else None
+    sim = sims[0] if args.plain else A.Simulation(scenes, max_steps=S, device=local, autotune=args.autotune)
     series = np.zeros((n_src, S), np.float32)
     k = 0
     for sc in cfg["scenes"]:
@@ -439,6 +440,7 @@ def main():
             "gpu_launches": launches,
             "kernels_per_step": kps,
             "clocks": clk}
+    line["config"]["layout"] = sim.layout
     if args.plain:
         line["config"]["parallelism"] = "plain: one context per scene, run one after another"
     if not args.no_adjoint and not args.plain:

@@ -168,7 +168,9 @@ typedef struct ard_options {
   int64_t max_steps;     /* capacity of source series and recorder history */
   int32_t use_graphs;    /* capture step sequences in CUDA graphs (default 1) */
   int32_t device;        /* CUDA device ordinal */
-  int32_t autotune;      /* pick kernel tile shapes per extent by timing (default 0) */
+  int32_t autotune;      /* nonzero: build each candidate layout (modal tile counts,
+                            lanes per ky row, fused or GEMM face transforms), time
+                            128 steps of each, keep the fastest (default 0) */
   int32_t arithmetic;    /* ARD_ARITH_ACCURATE (default) or ARD_ARITH_REFERENCE */
   int32_t adjoint;       /* nonzero: allocate the adjoint state (needed by ard_adjoint) */
 } ard_options;
@@ -294,6 +296,11 @@ int ard_last_error(const ard_ctx* ctx, char* buf, int64_t n);
  * step launches (the step's CUDA graph holds this many kernel nodes per
  * step, plus one counter kernel per 32 steps). */
 int ard_kernels_per_step(const ard_ctx* ctx, int32_t* out);
+
+/* Introspection, no counterpart in the reference: the layout the context
+ * uses (modal tiling, face-transform path; with options.autotune, every
+ * candidate's measured microseconds per step), as text. */
+int ard_describe(const ard_ctx* ctx, char* buf, int64_t n);
 
 /* Library version / ABI check. */
 int ard_abi_version(void);

@@ -202,3 +202,24 @@ def test_contexts_with_different_layer_sizes_interleave():
     big.run(40)
     assert big.time_step == 48 and small.time_step == 16
     assert np.isfinite(big.recorders()).all() and np.abs(big.recorders()).max() > 0
+
+
+def test_autotuned_context_matches_default():
+    """The autotuner only changes the tiling (summation order): same recorders
+    to rounding, and it reports the candidates it timed."""
+    g = load_run("multi4")
+    sc = g["scene"]
+    p = sc["params"]
+    scene = A.build_scene(sc["air"], sc["sources"], sc["recorders"], p["dh"], p["dt"], p["c0"], p["pml_layers"])
+    T = sc["steps"]
+    out = []
+    for tune in (False, True):
+        sim = A.Simulation(scene, max_steps=T, autotune=tune)
+        for i, s in enumerate(g["sources"]):
+            sim.set_source_series(i, s[:T])
+        sim.run(T)
+        out.append(sim.recorders(f64=True))
+        if tune:
+            assert sim.layout.startswith("autotuned") and "us/step" in sim.layout
+            assert sim.time_step == T
+    assert rel_l2(out[1][:, 0], out[0][:, 0]) < 1e-5
