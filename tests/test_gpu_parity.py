@@ -223,3 +223,26 @@ def test_autotuned_context_matches_default():
             assert sim.layout.startswith("autotuned") and "us/step" in sim.layout
             assert sim.time_step == T
     assert rel_l2(out[1][:, 0], out[0][:, 0]) < 1e-5
+
+
+def test_gemm_face_transforms_fp64_match_oracle():
+    """A 100 x 100 face in FP64 does not fit the fused face kernel's shared
+    memory: the two-pass GEMM transforms run; FP64 GPU against the FP64 C
+    oracle to 1e-10."""
+    dh, c0 = 0.1, 343.0
+    dt = float(np.float32(0.5 * dh / (c0 * np.sqrt(3.0))))
+    air, srcs, recs = [(0, 0, 0, 100, 100, 16)], [(30, 40, 8)], [(60, 55, 8), (20, 80, 7)]
+    T = 30
+    series = (np.hanning(T) * 1e3).astype(np.float32)
+    flat = O.make_flat_scene(air, srcs, recs, dict(dh=dh, dt=dt, c0=c0, pml_layers=5))
+    ref = O.OracleSim(flat, "f64")
+    ref.set_source_series(0, series)
+    ref.step(T)
+    want = ref.recorders()
+    sim = A.Simulation(A.build_scene(air, srcs, recs, dh, dt, c0, 5), precision=A.PREC_F64, max_steps=T)
+    assert "gemm" in sim.layout
+    sim.set_source_series(0, series)
+    sim.run(T)
+    got = sim.recorders(f64=True)
+    for r in range(want.shape[1]):
+        assert rel_l2(got[:, r], want[:, r]) < F64_TOL, r
