@@ -99,6 +99,18 @@ struct SideDev {
   int ou, ov;   // global (u, v) of the side's origin
   int ext;      // extent along the crossing axis
   int self;     // include_self_terms_
+  // Direct addressing (filled at layout time, so the interface kernel reads
+  // no partition tables): pressure of the n-th stencil layer (crossing
+  // coordinate ext-3+n on the lo side, n on the hi side) at (u, v) is
+  // pb[n][parity] + v * psv + u; the force of crossing coordinate c is, for
+  // a PML side, fb + c * fls + v * fsv + u, for an air side the shell cell
+  // of the layers fx / fy / fz of an extent-(w, h, d) partition (pitch wp).
+  long long pb[3][2];
+  int psv;
+  int fsv;
+  long long fb, fls;
+  long long fx, fy, fz;
+  int w, h, d, wp;
 };
 
 struct IfaceDev {

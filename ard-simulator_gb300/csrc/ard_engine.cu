@@ -381,8 +381,8 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   }
   ARD_CUDA(mark(kStageIface));
   if (ctx->n_face_cells > 0) {
-    IfaceArgs<T> ia{buf, ctx->d_ifs, (int)ctx->ifs.size(), ctx->n_face_cells, ctx->d_dct, ctx->d_pml,
-                    ctx->d_mask, par, (T)ctx->c0, (T)ctx->dh};
+    IfaceArgs<T> ia{buf, ctx->d_ifs, ctx->d_cell_iface, ctx->n_face_cells, ctx->d_mask, par, (T)ctx->c0,
+                    (T)ctx->dh};
     iface_kernel<T><<<grid_for(ctx->n_face_cells, 256, ctx->num_sms * 16), 256, 0, s>>>(ia);
     ARD_CUDA(cudaGetLastError());
   }

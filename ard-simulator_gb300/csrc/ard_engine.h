@@ -55,6 +55,7 @@ struct Ctx {
   std::vector<int4> pml_blocks;
   std::vector<IfaceDev> ifs;
   std::vector<unsigned char> masks;
+  std::vector<int> cell_iface;              // interface of every face cell
   std::vector<PointDev> srcpts, recpts;
   std::vector<int4> tiles;
   JobList fwd1, fwd2, inv1, inv2;           // two-pass GEMM face transforms
@@ -96,6 +97,7 @@ struct Ctx {
   PmlDev* d_pml = nullptr;
   int4* d_pml_blocks = nullptr;
   IfaceDev* d_ifs = nullptr;
+  int* d_cell_iface = nullptr;
   PointDev* d_srcpts = nullptr;
   PointDev* d_recpts = nullptr;
   int4* d_tiles = nullptr;

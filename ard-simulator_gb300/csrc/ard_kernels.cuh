@@ -283,14 +283,16 @@ __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
     }
     const SumJob J = a.jobs[lo];
     const T* p = buf + J.base + (g - J.first);
-    T v[4] = {0, 0, 0, 0};
+    T v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int b = 0;
-    for (; b + 4 <= J.nb; b += 4) {
+    for (; b + 8 <= J.nb; b += 8) {
 #pragma unroll
-      for (int k = 0; k < 4; ++k) v[k] += p[(long long)(b + k) * J.stride];
+      for (int k = 0; k < 8; ++k) v[k] += p[(long long)(b + k) * J.stride];
     }
-    for (; b < J.nb; ++b) v[0] += p[(long long)b * J.stride];
-    buf[J.base + (g - J.first)] = (v[0] + v[1]) + (v[2] + v[3]);
+#pragma unroll
+    for (int k = 0; k < 7; ++k)
+      if (b + k < J.nb) v[k] += p[(long long)(b + k) * J.stride];
+    buf[J.base + (g - J.first)] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
   }
 }
 
@@ -1041,42 +1043,27 @@ template <typename T>
 struct IfaceArgs {
   T* buf;
   const IfaceDev* ifs;
-  int nif;
+  const int* cell_iface;   // interface of every face cell
   long long total;
-  const DctDev* dct;
-  const PmlDev* pml;
   const unsigned char* masks;
   int par;
   T c0, dh;
 };
 
-// Pressure of one side at crossing coordinate c and face coordinates (u, v).
-template <typename T>
-__device__ __forceinline__ T side_pressure(const IfaceArgs<T>& a, int type, const SideDev& s, int c, int u, int v) {
-  if (s.kind == 0) {
-    const DctDev& D = a.dct[s.idx];
-    const int layer = face_layer(c, s.ext);
-    if (type == 0) return a.buf[D.pX + ((long long)layer * D.d + v) * D.h + u];
-    if (type == 1) return a.buf[D.pY + ((long long)layer * D.d + v) * D.wp + u];
-    return a.buf[D.pZ + ((long long)layer * D.h + v) * D.wp + u];
-  }
-  const PmlDev& P = a.pml[s.idx];
-  return a.buf[P.p[a.par] + ((long long)c * P.A + v) * P.B + u];
-}
-
-template <typename T>
-__device__ __forceinline__ void side_force(const IfaceArgs<T>& a, int type, const SideDev& s, int c, int u, int v, T val) {
-  if (s.kind == 0) {
-    const DctDev& D = a.dct[s.idx];
-    const int x = type == 0 ? c : u;
-    const int y = type == 0 ? u : (type == 1 ? c : v);
-    const int z = type == 2 ? c : v;
-    const long long o = shell_index(D, x, y, z);
-    if (o >= 0) a.buf[o] = val;
-    return;
-  }
-  const PmlDev& P = a.pml[s.idx];
-  a.buf[P.force + ((long long)(c - P.strip0) * P.A + v) * P.B + u] = val;
+// Offset of the force value of crossing coordinate c, face coordinates
+// (u, v) on side S (see SideDev), -1 for an air cell off the shell.
+__device__ __forceinline__ long long side_force_offset(const SideDev& S, int type, int c, int u, int v) {
+  if (S.kind == 1) return S.fb + (long long)c * S.fls + (long long)v * S.fsv + u;
+  const int x = type == 0 ? c : u;
+  const int y = type == 0 ? u : (type == 1 ? c : v);
+  const int z = type == 2 ? c : v;
+  int l = face_layer(x, S.w);
+  if (l >= 0) return S.fx + ((long long)l * S.d + z) * S.h + y;
+  l = face_layer(y, S.h);
+  if (l >= 0) return S.fy + ((long long)l * S.d + z) * S.wp + x;
+  l = face_layer(z, S.d);
+  if (l >= 0) return S.fz + ((long long)l * S.h + y) * S.wp + x;
+  return -1;
 }
 
 // Boundary::ComputeForcingTerms (boundary.cpp:21-173) for every face cell of
@@ -1086,14 +1073,10 @@ template <typename T>
 __global__ void __launch_bounds__(256) iface_kernel(IfaceArgs<T> a) {
   const T C[6][6] = {{0, 0, -2, 2, 0, 0},       {0, -2, 27, -27, 2, 0},     {-2, 27, -270, 270, -27, 2},
                      {2, -27, 270, -270, 27, -2}, {0, 2, -27, 27, -2, 0},     {0, 0, 2, -2, 0, 0}};
+  const T k0 = a.c0 * a.c0 / ((T)180 * a.dh * a.dh);
   for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < a.total;
        g += (long long)gridDim.x * blockDim.x) {
-    int lo = 0, hi = a.nif - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (a.ifs[mid].cell0 <= g) lo = mid; else hi = mid - 1;
-    }
-    const IfaceDev& I = a.ifs[lo];
+    const IfaceDev& I = a.ifs[a.cell_iface[g]];
     const long long local = g - I.cell0;
     const int nu = I.u1 - I.u0;
     const int iu = I.u0 + (int)(local % nu);
@@ -1104,11 +1087,9 @@ __global__ void __launch_bounds__(256) iface_kernel(IfaceArgs<T> a) {
     T pl[3], ph[3];
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
-      pl[n] = side_pressure(a, I.type, I.lo, I.lo.ext - 3 + n, lu, lv);
-      ph[n] = side_pressure(a, I.type, I.hi, n, hu, hv);
+      pl[n] = a.buf[I.lo.pb[n][a.par] + (long long)lv * I.lo.psv + lu];
+      ph[n] = a.buf[I.hi.pb[n][a.par] + (long long)hv * I.hi.psv + hu];
     }
-    const T c2 = a.c0 * a.c0;
-    const T d180 = (T)180 * a.dh * a.dh;
     const T absorp = (T)I.absorption;
 #pragma unroll
     for (int m = -3; m < 3; ++m) {
@@ -1118,15 +1099,16 @@ __global__ void __launch_bounds__(256) iface_kernel(IfaceArgs<T> a) {
       for (int n = 0; n < 3; ++n) sip1 += C[m + 3][n] * pl[n];
 #pragma unroll
       for (int n = 3; n < 6; ++n) sip2 += C[m + 3][n] * ph[n - 3];
+      long long o;
+      T sip;
       if (m < 0) {
-        const T sip = I.lo.self ? (sip1 + sip2) : sip2;
-        const T fi = sip * c2 / d180;
-        side_force(a, I.type, I.lo, I.lo.ext + m, lu, lv, absorp * fi);
+        sip = I.lo.self ? (sip1 + sip2) : sip2;
+        o = side_force_offset(I.lo, I.type, I.lo.ext + m, lu, lv);
       } else {
-        const T sip = I.hi.self ? (sip1 + sip2) : sip1;
-        const T fi = sip * c2 / d180;
-        side_force(a, I.type, I.hi, m, hu, hv, absorp * fi);
+        sip = I.hi.self ? (sip1 + sip2) : sip1;
+        o = side_force_offset(I.hi, I.type, m, hu, hv);
       }
+      if (o >= 0) a.buf[o] = absorp * (sip * k0);
     }
   }
 }

@@ -586,6 +586,37 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         ctx->masks.push_back(bits);
       }
     ctx->n_face_cells += (long long)(I.u1 - I.u0) * (I.v1 - I.v0);
+    for (int side = 0; side < 2; ++side) {
+      SideDev& S = side ? I.hi : I.lo;
+      for (int n = 0; n < 3; ++n) {
+        const int c = side == 0 ? S.ext - 3 + n : n;
+        if (S.kind == 0) {
+          const DctDev& D = ctx->dct[S.idx];
+          const int L = face_layer(c, S.ext);
+          long long b;
+          if (I.type == 0) { b = D.pX + (long long)L * D.d * D.h; S.psv = D.h; }
+          else if (I.type == 1) { b = D.pY + (long long)L * D.d * D.wp; S.psv = D.wp; }
+          else { b = D.pZ + (long long)L * D.h * D.wp; S.psv = D.wp; }
+          S.pb[n][0] = S.pb[n][1] = b;
+        } else {
+          const PmlDev& P = ctx->pml[S.idx];
+          S.pb[n][0] = P.p[0] + (long long)c * P.A * P.B;
+          S.pb[n][1] = P.p[1] + (long long)c * P.A * P.B;
+          S.psv = P.B;
+        }
+      }
+      if (S.kind == 0) {
+        const DctDev& D = ctx->dct[S.idx];
+        S.fx = D.fX; S.fy = D.fY; S.fz = D.fZ;
+        S.w = D.w; S.h = D.h; S.d = D.d; S.wp = D.wp;
+      } else {
+        const PmlDev& P = ctx->pml[S.idx];
+        S.fls = (long long)P.A * P.B;
+        S.fb = P.force - (long long)P.strip0 * S.fls;
+        S.fsv = P.B;
+      }
+    }
+    for (long long k = 0; k < (long long)(I.u1 - I.u0) * (I.v1 - I.v0); ++k) ctx->cell_iface.push_back((int)ctx->ifs.size());
     ctx->ifs.push_back(I);
   }
   for (size_t k = 0; k < ctx->pml.size(); ++k) {
@@ -738,6 +769,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   if ((rc = up(&ctx->d_pml, ctx->pml))) return rc;
   if ((rc = up(&ctx->d_pml_blocks, ctx->pml_blocks))) return rc;
   if ((rc = up(&ctx->d_ifs, ctx->ifs))) return rc;
+  if ((rc = up(&ctx->d_cell_iface, ctx->cell_iface))) return rc;
   if ((rc = up(&ctx->d_srcpts, ctx->srcpts))) return rc;
   if ((rc = up(&ctx->d_recpts, ctx->recpts))) return rc;
   if ((rc = up(&ctx->d_tiles, ctx->tiles))) return rc;
@@ -805,7 +837,8 @@ void free_ctx_device(Ctx* ctx) {
                   ctx->d_recpts, ctx->d_tiles, ctx->d_fwd1, ctx->d_fwd2, ctx->d_inv1, ctx->d_inv2, ctx->d_fwd2d,
                   ctx->d_inv2d, ctx->d_series,
                   ctx->d_hist, ctx->d_t, ctx->d_adj1_2d, ctx->d_adj2_2d, ctx->d_adjg[0], ctx->d_adjg[1],
-                  ctx->d_adjg[2], ctx->d_adjg[3], ctx->d_tb, ctx->d_phist, ctx->d_psum};
+                  ctx->d_adjg[2], ctx->d_adjg[3], ctx->d_tb, ctx->d_phist, ctx->d_psum,
+                  ctx->d_cell_iface};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
