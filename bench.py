@@ -19,6 +19,8 @@ extra work, not counted.
           against the measured HBM copy bandwidth
   cpu_baseline  the oracle (C restatement of the reference's CPU solver,
           FP32, OpenMP over partitions) on a bounded sample of the same scene
+  accuracy  FP32 recorders against the FP64 GPU path (same kernels in
+          double) on a bounded sample of the workload
   adjoint the forward + adjoint of the recorder misfit on the same workload
           (gradients w.r.t. source series, initial pressure and the six PML
           face scales; target from a seeded perturbed source, face scales
@@ -181,6 +183,40 @@ def run_reference_arm(args, rank):
     return 0
 
 
+def accuracy_measurement(A, cfg, scenes, args, device):
+    """Recorder error of the FP32 product path against the FP64 GPU oracle
+    (the same kernels in double) on a bounded sample: the first 16 scenes,
+    min(steps, 2000) steps for multi-scene or c4-size workloads, the whole
+    run otherwise.  Relative L2 per recorder; the max is reported."""
+    S = cfg["steps"]
+    n_air = sum(s.air_cells for s in scenes)
+    big = len(scenes) > 1 or n_air > 5e7
+    T = min(S, 2000) if big else S
+    sub = scenes[:16]
+    subcfg = cfg["scenes"][:16]
+    out = []
+    for prec in (A.PREC_F32, A.PREC_F64):
+        sim = A.Simulation(sub, precision=prec, max_steps=T, device=device)
+        k = 0
+        for i, sc in enumerate(subcfg):
+            for j, srs in enumerate(sc["series"]):
+                sim.set_source_series(j, srs[:T], scene=i)
+        sim.run(T)
+        out.append(sim.recorders(scene=-1, f64=True))
+        sim.close()
+    a, b = out
+    # recorders the wave has reached: RMS above 1e-3 of the loudest recorder's (the others
+    # hold only the rounding noise of the global modal transforms, where a relative error means nothing)
+    rms = np.sqrt(np.mean(b ** 2, axis=0))
+    live = [r for r in range(b.shape[1]) if rms[r] > 1e-3 * rms.max()]
+    errs = [float(np.linalg.norm(a[:, r] - b[:, r]) / np.linalg.norm(b[:, r])) for r in live]
+    return {"rel_l2_vs_fp64_max": max(errs) if errs else None, "recorders": len(live),
+            "recorders_total": int(b.shape[1]),
+            "rel_l2_vs_fp64_all": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)),
+            "sample": f"{len(sub)} scene(s), {T} steps, FP32 accurate arithmetic vs FP64 GPU; max over recorders "
+                      f"whose RMS is above 1e-3 of the loudest"}
+
+
 def adjoint_measurement(A, cfg, scenes, args, device):
     """Forward + adjoint of the recorder misfit (gradients w.r.t. the source
     series, the initial pressure and the six PML face scales) against the
@@ -254,6 +290,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=6, help="time steps per reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=None, help="steps of the adjoint measurement (default: sim steps)")
     ap.add_argument("--checkpoint-every", type=int, default=0,
                     help="adjoint checkpoint interval (0: keep the whole PML history when it fits, else automatic)")
@@ -405,7 +442,8 @@ def main():
     stages = sim.profile(prof_steps, stream=handle)
     peak, peak_kind = peaks()
     modal_ms = stages[MODAL_STAGE]
-    alg_bytes = BYTES_PER_AIR_CELL * n_air
+    # the profiled context: the batch, or (plain) the first scene's own context
+    alg_bytes = BYTES_PER_AIR_CELL * (scenes[0].air_cells if args.plain else n_air)
     achieved = alg_bytes / (modal_ms / 1e3) / 1e9 if modal_ms > 0 else 0.0
     traffic = None
     tpath = os.path.join(ROOT, "profiles", f"traffic_{args.config}.txt")
@@ -441,6 +479,8 @@ def main():
             "kernels_per_step": kps,
             "clocks": clk}
     line["config"]["layout"] = sim.layout
+    if not args.no_accuracy and not args.plain:
+        line["accuracy"] = accuracy_measurement(A, cfg, scenes, args, local)
     if args.plain:
         line["config"]["parallelism"] = "plain: one context per scene, run one after another"
     if not args.no_adjoint and not args.plain:
