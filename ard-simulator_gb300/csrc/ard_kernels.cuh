@@ -121,9 +121,12 @@ __device__ __forceinline__ T job_input(const T* __restrict__ buf, const XformJob
 template <typename T>
 __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, const XformJob* __restrict__ jobs,
                                                           int njobs, int total) {
-  // two K-chunk buffers: chunk k+1 is fetched into registers while chunk k is multiplied
-  __shared__ __align__(16) T Ps[2][16][64 + 4];  // P(m0 + mm, k0 + kk) at [kk][mm]
-  __shared__ __align__(16) T Qs[2][16][64 + 4];  // Q(k0 + kk, n0 + nn) at [kk][nn]
+  // two K-chunk buffers: chunk k+1 is fetched into registers while chunk k is
+  // multiplied; chunks of 16 k (32 measured slower)
+  constexpr int BK = 16;
+  constexpr int NR = BK / 4;                     // elements of each operand a thread stages per chunk
+  __shared__ __align__(16) T Ps[2][BK][64 + 4];  // P(m0 + mm, k0 + kk) at [kk][mm]
+  __shared__ __align__(16) T Qs[2][BK][64 + 4];  // Q(k0 + kk, n0 + nn) at [kk][nn]
   const int tid = threadIdx.x;
   const int ty = tid >> 4, tx = tid & 15;
   for (int unit = blockIdx.x; unit < total; unit += gridDim.x) {
@@ -134,15 +137,15 @@ __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, co
     const int Nd = J.rows ? J.n : J.batch;
     const int K = J.n;
     const T* A = buf + J.ctab;
-    T pr[4], qr[4];
+    T pr[NR], qr[NR];
     // global -> registers for the chunk at k0
     auto fetch = [&](int k0) {
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
+      for (int r = 0; r < NR; ++r) {
         const int e = tid + 256 * r;
         if (!J.rows) {
           // P = A (m = output o, k = j); Q = X (k = j, n = column)
-          const int mm = J.inverse ? (e & 63) : (e >> 4), kk = J.inverse ? (e >> 6) : (e & 15);
+          const int mm = J.inverse ? (e & 63) : (e / BK), kk = J.inverse ? (e >> 6) : (e % BK);
           const int m = m0 + mm, k = k0 + kk;
           T pv = 0;
           if (m < Md && k < K) pv = J.inverse ? A[(long long)k * K + m] : A[(long long)m * K + k];
@@ -152,10 +155,10 @@ __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, co
           qr[r] = (n < Nd && kk2 < K) ? job_input(buf, J, (long long)kk2 * J.ld + n) : (T)0;
         } else {
           // P = X (m = line, k = j); Q(k, n) = A(n, k)
-          const int mm = e >> 4, kk = e & 15;
+          const int mm = e / BK, kk = e % BK;
           const int m = m0 + mm, k = k0 + kk;
           pr[r] = (m < Md && k < K) ? job_input(buf, J, (long long)m * J.ld + k) : (T)0;
-          const int nn = J.inverse ? (e & 63) : (e >> 4), kq = J.inverse ? (e >> 6) : (e & 15);
+          const int nn = J.inverse ? (e & 63) : (e / BK), kq = J.inverse ? (e >> 6) : (e % BK);
           const int n = n0 + nn, kk2 = k0 + kq;
           T qv = 0;
           if (n < Nd && kk2 < K) qv = J.inverse ? A[(long long)kk2 * K + n] : A[(long long)n * K + kk2];
@@ -165,15 +168,15 @@ __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, co
     };
     auto commit = [&](int sb) {
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
+      for (int r = 0; r < NR; ++r) {
         const int e = tid + 256 * r;
         if (!J.rows) {
-          const int mm = J.inverse ? (e & 63) : (e >> 4), kk = J.inverse ? (e >> 6) : (e & 15);
+          const int mm = J.inverse ? (e & 63) : (e / BK), kk = J.inverse ? (e >> 6) : (e % BK);
           Ps[sb][kk][mm] = pr[r];
           Qs[sb][e >> 6][e & 63] = qr[r];
         } else {
-          Ps[sb][e & 15][e >> 4] = pr[r];
-          const int nn = J.inverse ? (e & 63) : (e >> 4), kq = J.inverse ? (e >> 6) : (e & 15);
+          Ps[sb][e % BK][e / BK] = pr[r];
+          const int nn = J.inverse ? (e & 63) : (e / BK), kq = J.inverse ? (e >> 6) : (e % BK);
           Qs[sb][kq][nn] = qr[r];
         }
       }
@@ -188,11 +191,11 @@ __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, co
     commit(0);
     __syncthreads();
     int sb = 0;
-    for (int k0 = 0; k0 < K; k0 += 16) {
-      const bool more = k0 + 16 < K;
-      if (more) fetch(k0 + 16);
+    for (int k0 = 0; k0 < K; k0 += BK) {
+      const bool more = k0 + BK < K;
+      if (more) fetch(k0 + BK);
 #pragma unroll
-      for (int kk = 0; kk < 16; ++kk) {
+      for (int kk = 0; kk < BK; ++kk) {
         T pa[4], qb[4];
         load4(&Ps[sb][kk][ty * 4], pa);
         load4(&Qs[sb][kk][tx * 4], qb);

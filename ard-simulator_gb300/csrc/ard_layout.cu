@@ -359,7 +359,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   for (DctDev& D : ctx->dct) {
     const int need = std::min(D.wp, 128) / 4;
     D.G = need <= 8 ? 8 : (need <= 16 ? 16 : 32);
-    if (ctx->tune_g_shift && D.G > 8) D.G /= 2;
+    for (int k = 0; k < ctx->tune_g_shift && D.G > 8; ++k) D.G /= 2;
     D.kxt = 4 * D.G;
     D.rpc = kModalThreads / D.G;
     D.nbx = (D.wp + D.kxt - 1) / D.kxt;
