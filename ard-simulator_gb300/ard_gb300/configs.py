@@ -17,6 +17,7 @@ exceeds the 6th-order PML leapfrog limit of 0.470).
   c3  c1 geometry for forward + adjoint
   c4  40 x 25 m footprint, 12 m deep, 24 seeded partitions at h = 0.04
       (~1.9e8 cells), 10-cell PML, 16 recorders, 20000 steps
+  c4one  the largest c4 partition alone (profiling case, 12.4 M cells)
 """
 from __future__ import annotations
 
@@ -87,6 +88,13 @@ def config(name, steps=None, seed=1):
         rec = pick_points(rng, air, 16)
         return dict(name=name, h=h, c0=C_SOUND, dt=dt_cfl(h), pml=10, steps=n,
                     scenes=[dict(air=air, sources=src, recorders=rec, series=[gaussian_pulse(n)])])
+    if name == "c4one":
+        # profiling case: the largest c4 partition alone (232 x 178 x 300 cells at h = 0.04)
+        h = 0.04
+        n = steps or 200
+        air = [(0, 0, 0, 232, 178, 300)]
+        sc = dict(air=air, sources=[(40, 50, 150)], recorders=[(180, 120, 100)], series=[gaussian_pulse(n)])
+        return dict(name=name, h=h, c0=C_SOUND, dt=dt_cfl(h), pml=10, steps=n, scenes=[sc])
     raise ValueError(name)
 
 

@@ -126,14 +126,11 @@ struct IfaceDev {
 //   cols (rows == 0): lines are columns of [n][ld];  Out = A X,   M = n, N = batch
 //   rows (rows == 1): lines are rows of [batch][ld]; Out = X A^T, M = batch, N = n
 // A(o, j) = C[o][j] (forward, REDFT10) or Ci[j][o] (inverse, REDFT01); ctab
-// points at the matrix used.  X = sum over `nparts` slabs (stride
-// part_stride) of in0 + sgn * in1 (in1 < 0: absent).
+// points at the matrix used.  X = in0 + sgn * in1 (in1 < 0: absent).
 struct XformJob {
   long long in0, in1;
   long long out;
   long long ctab;
-  long long part_stride;
-  int nparts;
   int sgn;
   int n;
   int batch;

@@ -171,7 +171,7 @@ extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_o
   // Autotuner: build the context for each candidate layout, time real steps
   // (CUDA graphs, the production path), keep the fastest.
   struct Cand { int tiles, gshift, gemm; };
-  const Cand cands[] = {{1, 0, 0}, {2, 0, 0}, {4, 0, 0}, {1, 1, 0}, {2, 1, 0}, {1, 2, 0}, {2, 2, 0}, {1, 0, 1}};
+  const Cand cands[] = {{1, 2, 0}, {2, 2, 0}, {4, 2, 0}, {1, 1, 0}, {2, 1, 0}, {1, 0, 0}, {2, 0, 0}, {1, 2, 1}};
   std::unique_ptr<Ctx> best;
   float best_ms = 0.f;
   std::string report;

@@ -78,7 +78,7 @@ struct Ctx {
   bool adjoint = false;
   // layout choices (the autotuner varies them; defaults are the heuristics)
   int tune_tiles = 1;      // modal tiles per wave slot (x 2 per SM): kz split finer when > 1
-  int tune_g_shift = 0;    // k > 0: ky rows k lane-sizes narrower (more kx tiles, more ky rows per tile)
+  int tune_g_shift = 2;    // k > 0: ky rows k lane-sizes narrower (more kx tiles, more ky rows per tile)
   int tune_gemm = 0;       // 1: two-pass GEMM face transforms even when the fused ones fit
   std::string tuning;      // description of the chosen layout
   // adjoint face transforms (options.adjoint): fused 2D jobs and the two-pass

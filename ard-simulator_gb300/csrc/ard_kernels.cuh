@@ -109,13 +109,8 @@ __device__ __forceinline__ int find_job(const XformJob* __restrict__ jobs, int n
 
 template <typename T>
 __device__ __forceinline__ T job_input(const T* __restrict__ buf, const XformJob& J, long long off) {
-  T v = 0;
-  for (int b = 0; b < J.nparts; ++b) {
-    const long long o = (long long)b * J.part_stride + off;
-    v += buf[J.in0 + o];
-    if (J.in1 >= 0) v += (T)J.sgn * buf[J.in1 + o];
-  }
-  return v;
+  const T a = buf[J.in0 + off];
+  return J.in1 >= 0 ? a + (T)J.sgn * buf[J.in1 + off] : a;
 }
 
 template <typename T>

@@ -206,24 +206,24 @@ void build_adjoint_jobs(Ctx* ctx) {
           XformJob j{};   // rows along U with Ci_U: A(o, j) = Ci_U[o][j]
           j.in0 = a.q + n * LS; j.in1 = a.q + (5 - n) * LS; j.sgn = pm ? -1 : 1;
           j.out = a.tmp + (pm * 3 + n) * LS; j.ctab = a.cU + UU; j.n = a.U; j.batch = a.V; j.ld = a.ld;
-          j.nparts = 1; j.part_stride = 0; j.inverse = 0; j.rows = 1; j.scale = 1.0;
+          j.inverse = 0; j.rows = 1; j.scale = 1.0;
           add_job(ctx->adjg[0], j);
           XformJob k{};   // columns along V with Ci_V
           k.in0 = a.tmp + (pm * 3 + n) * LS; k.in1 = -1; k.sgn = 1;
           k.out = a.P + (pm * 3 + n) * LS; k.ctab = a.cV + VV; k.n = a.V; k.batch = a.U; k.ld = a.ld;
-          k.nparts = 1; k.part_stride = 0; k.inverse = 0; k.rows = 0; k.scale = D.si;
+          k.inverse = 0; k.rows = 0; k.scale = D.si;
           add_job(ctx->adjg[1], k);
         }
       for (int L = 0; L < 6; ++L) {
         const int n = L < 3 ? L : 5 - L;
         XformJob j{};     // columns along V with C_V^T: A(o, r) = C_V[r][o]
         j.in0 = a.R + (0 * 3 + n) * LS; j.in1 = a.R + (1 * 3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
-        j.nparts = 1; j.part_stride = 0;   // partials summed beforehand (post_modal_kernel)
+       
         j.out = a.tmp + L * LS; j.ctab = a.cV; j.n = a.V; j.batch = a.U; j.ld = a.ld;
         j.inverse = 1; j.rows = 0; j.scale = 1.0;
         add_job(ctx->adjg[2], j);
         XformJob k{};     // rows along U with C_U: A(o, j) = C_U[j][o]
-        k.in0 = a.tmp + L * LS; k.in1 = -1; k.sgn = 1; k.nparts = 1; k.part_stride = 0;
+        k.in0 = a.tmp + L * LS; k.in1 = -1; k.sgn = 1;
         k.out = a.a + L * LS; k.ctab = a.cU; k.n = a.U; k.batch = a.V; k.ld = a.ld;
         k.inverse = 1; k.rows = 1; k.scale = D.sf;
         add_job(ctx->adjg[3], k);
@@ -661,24 +661,24 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
           XformJob j{};
           j.in0 = a.f + n * LS; j.in1 = a.f + (5 - n) * LS; j.sgn = pm ? -1 : 1;
           j.out = a.tmp + (pm * 3 + n) * LS; j.ctab = a.cU; j.n = a.nU; j.batch = a.nV; j.ld = a.ld;
-          j.nparts = 1; j.part_stride = 0; j.inverse = 0; j.rows = 1; j.scale = 1.0;
+          j.inverse = 0; j.rows = 1; j.scale = 1.0;
           add_job(ctx->fwd1, j);
           XformJob k{};
           k.in0 = a.tmp + (pm * 3 + n) * LS; k.in1 = -1; k.sgn = 1;
           k.out = a.P + (pm * 3 + n) * LS; k.ctab = a.cV; k.n = a.nV; k.batch = a.nU; k.ld = a.ld;
-          k.nparts = 1; k.part_stride = 0; k.inverse = 0; k.rows = 0; k.scale = D.sf;
+          k.inverse = 0; k.rows = 0; k.scale = D.sf;
           add_job(ctx->fwd2, k);
         }
       for (int L = 0; L < 6; ++L) {
         const int n = L < 3 ? L : 5 - L;
         XformJob j{};
         j.in0 = a.R + (0 * 3 + n) * LS; j.in1 = a.R + (1 * 3 + n) * LS; j.sgn = L < 3 ? 1 : -1;
-        j.nparts = 1; j.part_stride = 0;   // partials summed beforehand (post_modal_kernel)
+       
         j.out = a.tmp + L * LS; j.ctab = a.cV + (long long)a.nV * a.nV; j.n = a.nV; j.batch = a.nU; j.ld = a.ld;
         j.inverse = 1; j.rows = 0; j.scale = 1.0;
         add_job(ctx->inv1, j);
         XformJob k{};
-        k.in0 = a.tmp + L * LS; k.in1 = -1; k.sgn = 1; k.nparts = 1; k.part_stride = 0;
+        k.in0 = a.tmp + L * LS; k.in1 = -1; k.sgn = 1;
         k.out = a.p + L * LS; k.ctab = a.cU + (long long)a.nU * a.nU; k.n = a.nU; k.batch = a.nV; k.ld = a.ld;
         k.inverse = 1; k.rows = 1; k.scale = D.si;
         add_job(ctx->inv2, k);
@@ -875,7 +875,7 @@ int dense_transform_ex(Ctx* ctx, const DctDev& D, long long in, long long out, l
   };
   auto make = [&](long long i0, long long o0, int n, int batch, int ld, int rows, double sc) {
     XformJob j{};
-    j.in0 = i0; j.in1 = -1; j.sgn = 1; j.nparts = 1; j.part_stride = 0;
+    j.in0 = i0; j.in1 = -1; j.sgn = 1;
     j.out = o0; j.ctab = table(n); j.n = n; j.batch = batch; j.ld = ld;
     j.inverse = inverse ? 1 : 0; j.rows = rows; j.scale = sc;
     const int Md = rows ? batch : n, Nd = rows ? n : batch;

@@ -68,7 +68,7 @@ __global__ void build_jobs_kernel(XformJob* jobs, long long a, long long b, long
   auto make = [&](long long in0, long long out, long long tab, int n, int batch, int ld, int rows, double sc,
                   int first) {
     XformJob j{};
-    j.in0 = in0; j.in1 = -1; j.sgn = 1; j.nparts = 1; j.part_stride = 0;
+    j.in0 = in0; j.in1 = -1; j.sgn = 1;
     j.out = out; j.ctab = tab; j.n = n; j.batch = batch; j.ld = ld;
     j.inverse = 1; j.rows = rows; j.scale = sc;
     const int Md = rows ? batch : n, Nd = rows ? n : batch;
