@@ -371,16 +371,23 @@ __global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ 
     }
     __syncthreads();
     // ---- along U: T0 = E B, T1 = O B (lane = column, warp = row group) ----
+    // narrow jobs (16 columns): lanes 0-15 and 16-31 take the same columns on
+    // interleaved rows, so the warp stays fully busy
+    const int col = J.narrow ? (lane & 15) : lane;
+    const int rsub = J.narrow ? 8 * (lane >> 4) : 0;
+    const int rstr = J.narrow ? 16 : 8;
+    const int rstep = J.narrow ? 2 * kRowStep : kRowStep;
+    const int wrow0 = J.narrow ? (warp & 7) + 64 * (warp >> 3) : wrow;
     auto along_u = [&](auto de, auto dodd) {
       constexpr bool DE = decltype(de)::value, DO = decltype(dodd)::value;
-      for (int r0 = wrow; r0 < V; r0 += kRowStep) {
+      for (int r0 = wrow0 + rsub; r0 - rsub < V; r0 += rstep) {
         T e[4] = {0, 0, 0, 0}, o[4] = {0, 0, 0, 0};
         int rr[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) rr[i] = min(r0 + 8 * i, V - 1);
+        for (int i = 0; i < 4; ++i) rr[i] = min(r0 + rstr * i, V - 1);
         for (int j = 0; j < U; j += 4) {
-          const T b0 = Bs[j * 33 + lane], b1 = Bs[(j + 1) * 33 + lane];
-          const T b2 = Bs[(j + 2) * 33 + lane], b3 = Bs[(j + 3) * 33 + lane];
+          const T b0 = Bs[j * 33 + col], b1 = Bs[(j + 1) * 33 + col];
+          const T b2 = Bs[(j + 2) * 33 + col], b3 = Bs[(j + 3) * 33 + col];
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             T x[4], y[4];
@@ -396,9 +403,9 @@ __global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ 
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i)
-          if (r0 + 8 * i < V) {
-            if constexpr (DE) T0[(r0 + 8 * i) * 33 + lane] = e[i];
-            if constexpr (DO) T1[(r0 + 8 * i) * 33 + lane] = o[i];
+          if (r0 + rstr * i < V) {
+            if constexpr (DE) T0[(r0 + rstr * i) * 33 + col] = e[i];
+            if constexpr (DO) T1[(r0 + rstr * i) * 33 + col] = o[i];
           }
       }
     };
@@ -429,18 +436,18 @@ __global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ 
     const T scale = (T)J.scale;
     auto along_v = [&](auto de, auto dodd) {
       constexpr bool DE = decltype(de)::value, DO = decltype(dodd)::value;
-      for (int o0 = wrow; o0 < V; o0 += kRowStep) {
+      for (int o0 = wrow0 + rsub; o0 - rsub < V; o0 += rstep) {
         T e[4] = {0, 0, 0, 0}, od[4] = {0, 0, 0, 0};
         int oo[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) oo[i] = min(o0 + 8 * i, V - 1);
+        for (int i = 0; i < 4; ++i) oo[i] = min(o0 + rstr * i, V - 1);
         for (int r = 0; r < V; r += 4) {
           T t[4], u[4];
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             const bool ok = r + k < V;
-            if constexpr (DE) t[k] = ok ? T0[(r + k) * 33 + lane] : (T)0;
-            if constexpr (DO) u[k] = ok ? T1[(r + k) * 33 + lane] : (T)0;
+            if constexpr (DE) t[k] = ok ? T0[(r + k) * 33 + col] : (T)0;
+            if constexpr (DO) u[k] = ok ? T1[(r + k) * 33 + col] : (T)0;
           }
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
@@ -450,11 +457,11 @@ __global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ 
             if constexpr (DO) od[i] += a4[0] * u[0] + a4[1] * u[1] + a4[2] * u[2] + a4[3] * u[3];
           }
         }
-        if (lane < J.ub) {
+        if (col < J.ub) {
 #pragma unroll
           for (int i = 0; i < 4; ++i)
-            if (o0 + 8 * i < V) {
-              const long long off = (long long)(o0 + 8 * i) * J.ld + J.u0 + lane;
+            if (o0 + rstr * i < V) {
+              const long long off = (long long)(o0 + rstr * i) * J.ld + J.u0 + col;
               if constexpr (DE) buf[J.out0 + off] = e[i] * scale;
               if constexpr (DO) buf[J.out1 + off] = od[i] * scale;
             }

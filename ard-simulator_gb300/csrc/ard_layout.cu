@@ -147,16 +147,29 @@ int zero_state(Ctx* ctx) {
 // `slots` blocks: the launch lasts as long as its largest job.  Largest
 // first afterwards.
 void balance_face_jobs(std::vector<Face2DJob>* jobs, int slots) {
-  auto work = [](const Face2DJob& j) { return (long long)j.V * (j.U + j.V) * (j.which == 0 ? 2 : 1); };
+  // arithmetic of a job: both transforms over its columns, for one or two outputs
+  auto work = [](const Face2DJob& j) {
+    return (long long)j.V * (j.U + j.V) * (j.which == 0 ? 2 : 1) * (j.narrow ? 16 : 32);
+  };
+  for (Face2DJob& j : *jobs) j.narrow = j.ub <= 16 ? 1 : 0;
   while ((int)jobs->size() < slots && !jobs->empty()) {
     size_t k = 0;
     for (size_t i = 1; i < jobs->size(); ++i)
       if (work((*jobs)[i]) > work((*jobs)[k])) k = i;
-    if ((*jobs)[k].which != 0) break;   // the largest is already single: splitting others cannot help
-    Face2DJob b = (*jobs)[k];
-    (*jobs)[k].which = 1;
-    b.which = 2;
-    jobs->push_back(b);
+    Face2DJob& J = (*jobs)[k];
+    if (J.which == 0) {            // one block per output
+      Face2DJob b = J;
+      J.which = 1;
+      b.which = 2;
+      jobs->push_back(b);
+    } else if (!J.narrow) {        // two 16-column halves
+      Face2DJob b = J;
+      J.ub = 16; J.narrow = 1;
+      b.u0 += 16; b.ub -= 16; b.narrow = 1;
+      jobs->push_back(b);
+    } else {
+      break;                       // the largest job cannot be split further
+    }
   }
   std::stable_sort(jobs->begin(), jobs->end(),
                    [&](const Face2DJob& a, const Face2DJob& b) { return work(a) > work(b); });
