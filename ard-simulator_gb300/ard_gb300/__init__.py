@@ -106,6 +106,7 @@ SIGNATURES = {
                               C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "ard_read_initial_pressure_grad": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
     "ard_kernels_per_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "ard_write_outputs": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.c_int64]),
     "ard_describe": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     "ard_profile_steps": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "ard_last_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
@@ -389,6 +390,11 @@ class Simulation:
         out = np.zeros((q[7], q[6], q[5]), np.float32)
         self._c(lib().ard_read_initial_pressure_grad(self._h, scene, partition, _fptr(out)))
         return out
+
+    def write_outputs(self, directory, scene=0, nt=None):
+        """response_<r>.txt and source_<s>.txt in the reference's format (ard_write_outputs)."""
+        nt = self.time_step if nt is None else nt
+        self._c(lib().ard_write_outputs(self._h, scene, os.fsencode(directory), nt))
 
     def field(self, partition, scene=0):
         if not (0 <= scene < len(self.scenes)) or not (0 <= partition < self.scenes[scene].desc.n_partitions):

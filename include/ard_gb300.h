@@ -241,6 +241,15 @@ int ard_read_recorders_f64(ard_ctx* ctx, int32_t scene, double* out, int64_t t0,
  * partition this runs the full inverse transform of the current modes. */
 int ard_read_field(ard_ctx* ctx, int32_t scene, int32_t partition, float* out);
 
+/* Text output in the reference's formats (output/README.md): for scene
+ * `scene`, response_<r>.txt per recorder (the recorded pressure of steps
+ * 0 .. nt-1, one value per line, as Recorder::RecordField's response stream,
+ * recorder.cpp:15-16,55) and source_<s>.txt per source (the injected series,
+ * as SoundSource::RecordSource, sound_source.cpp:50-56), in directory `dir`
+ * (which must exist).  The per-step 10x10x10 neighbourhood file out_<r>.txt
+ * is not produced.  Synchronous. */
+int ard_write_outputs(ard_ctx* ctx, int32_t scene, const char* dir, int64_t nt);
+
 /* No counterpart in the reference.  The field readout of ard_read_field for
  * an air partition of an FP32 context, for callers that cannot allocate
  * device memory: it allocates nothing.  The caller passes a device buffer of

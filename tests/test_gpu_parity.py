@@ -246,3 +246,20 @@ def test_gemm_face_transforms_fp64_match_oracle():
     got = sim.recorders(f64=True)
     for r in range(want.shape[1]):
         assert rel_l2(got[:, r], want[:, r]) < F64_TOL, r
+
+
+def test_write_outputs_in_reference_format(tmp_path):
+    """response_<r>.txt / source_<s>.txt: one value per line, the recorder
+    history and the injected series (output/README.md)."""
+    g = load_run("scene2_gauss")
+    sc = g["scene"]
+    scene, sim = gpu_run(sc, g["sources"])
+    T = sim.time_step
+    sim.write_outputs(str(tmp_path))
+    rec = sim.recorders()
+    for r in range(rec.shape[1]):
+        vals = np.loadtxt(tmp_path / f"response_{r}.txt")
+        assert vals.shape == (T,)
+        np.testing.assert_allclose(vals, rec[:, r], rtol=1e-5, atol=1e-30)
+    src = np.loadtxt(tmp_path / "source_0.txt")
+    np.testing.assert_allclose(src, g["sources"][0][:T], rtol=1e-5)
