@@ -158,6 +158,7 @@ struct Face2DJob {
   int u0, ub;
   int which;     // 0: both outputs; 1: out0 only; 2: out1 only (a pair split over two blocks)
   int narrow;    // 1: at most 16 columns, two rows per lane pair
+  int part;      // air partition (engine index)
   double scale;
 };
 

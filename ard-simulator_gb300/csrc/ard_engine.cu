@@ -154,7 +154,7 @@ extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_o
   auto describe = [](const Ctx* c) {
     return std::string("tiles x") + std::to_string(c->tune_tiles) + ", lanes/row " +
            (c->tune_g_shift == 0 ? "fit" : (c->tune_g_shift == 1 ? "narrow" : "narrower")) + ", faces " + (c->fused_faces ? "fused" : "gemm") + ", " +
-           std::to_string(c->tiles.size()) + " modal tiles";
+           std::to_string(c->tiles.size()) + " modal tiles, " + std::to_string(c->ngroups) + " air stream(s)";
   };
   if (!autotune) {
     int rc = build_layout(ctx.get(), scenes, n_scenes);
@@ -266,10 +266,12 @@ extern "C" int ard_kernels_per_step(const ard_ctx* c, int32_t* out) {
   if (!c || !out) return ARD_ERR_INVALID;
   const Ctx* ctx = reinterpret_cast<const Ctx*>(c);
   int n = ctx->pml_blocks.empty() ? 0 : 1;
-  if (!ctx->dct.empty()) {
-    n += ctx->fused_faces ? 2 : 4;           // forward and inverse face transforms
-    n += 1;                                  // modal update
-    n += (ctx->recpts.empty() && ctx->psum.empty()) ? 0 : 1;   // recorder sums + partial sums
+  for (int g = 0; g < (ctx->dct.empty() ? 0 : ctx->ngroups); ++g) {
+    const Ctx::AirGroup& G = ctx->groups[g];
+    if (ctx->fused_faces) n += (G.f_hi > G.f_lo ? 1 : 0) + (G.i_hi > G.i_lo ? 1 : 0);   // face transforms
+    else n += 4;
+    n += G.t_hi > G.t_lo ? 1 : 0;                                                       // modal update
+    n += (G.r_hi > G.r_lo || G.s_total > 0) ? 1 : 0;                                    // recorder + partial sums
   }
   n += ctx->n_face_cells > 0 ? 1 : 0;        // interfaces
   *out = n;
@@ -332,47 +334,70 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   }
   if (!ctx->dct.empty()) {
     const int gx = ctx->num_sms * 4;
-    ARD_CUDA(mark(kStageFwdRows));
-    if (ctx->fused_faces) {
-      face2d_kernel<T><<<grid_for((long long)ctx->fwd2d.size(), 1, gx), kFace2DThreads, ctx->f2d_bytes, s>>>(
-          buf, ctx->d_fwd2d, (int)ctx->fwd2d.size(), ctx->f2d_smem);
-    } else {
-      xform_gemm_kernel<T><<<grid_for(ctx->fwd1.units, 1, gx), 256, 0, s>>>(buf, ctx->d_fwd1, (int)ctx->fwd1.jobs.size(),
-                                                                             ctx->fwd1.units);
-    }
-    ARD_CUDA(cudaGetLastError());
-    ARD_CUDA(mark(kStageFwdCols));
-    if (!ctx->fused_faces) {
-      xform_gemm_kernel<T><<<grid_for(ctx->fwd2.units, 1, gx), 256, 0, s>>>(buf, ctx->d_fwd2, (int)ctx->fwd2.jobs.size(),
-                                                                             ctx->fwd2.units);
-      ARD_CUDA(cudaGetLastError());
-    }
-    ModalArgs<T> ma{buf, ctx->d_dct, ctx->d_tiles, (int)ctx->tiles.size(), ctx->d_srcpts, ctx->d_recpts,
-                    ctx->d_series, ctx->max_steps, ctx->d_t, tstep, par};
-    ARD_CUDA(mark(kStageModal));
     const size_t msmem = kModalSmemElems * sizeof(T);
-    const int mgrid = grid_for((long long)ctx->tiles.size(), 1, ctx->num_sms * 2);
-    if (ctx->arith == ARD_ARITH_REFERENCE)
-      modal_kernel<T, true><<<mgrid, kModalThreads, msmem, s>>>(ma);
-    else
-      modal_kernel<T, false><<<mgrid, kModalThreads, msmem, s>>>(ma);
-    ARD_CUDA(cudaGetLastError());
-    ARD_CUDA(mark(kStageRecorder));
-    if (int rc = launch_post_modal<T>(ctx, s, tstep, true)) return rc;
-    ARD_CUDA(mark(kStageInvCols));
-    if (ctx->fused_faces) {
-      face2d_kernel<T><<<grid_for((long long)ctx->inv2d.size(), 1, gx), kFace2DThreads, ctx->f2d_bytes, s>>>(
-          buf, ctx->d_inv2d, (int)ctx->inv2d.size(), ctx->f2d_smem);
-    } else {
-      xform_gemm_kernel<T><<<grid_for(ctx->inv1.units, 1, gx), 256, 0, s>>>(buf, ctx->d_inv1, (int)ctx->inv1.jobs.size(),
-                                                                             ctx->inv1.units);
-    }
-    ARD_CUDA(cudaGetLastError());
-    ARD_CUDA(mark(kStageInvRows));
-    if (!ctx->fused_faces) {
-      xform_gemm_kernel<T><<<grid_for(ctx->inv2.units, 1, gx), 256, 0, s>>>(buf, ctx->d_inv2, (int)ctx->inv2.jobs.size(),
-                                                                             ctx->inv2.units);
+    // one stage of one group's air branch on stream `st`
+    auto stage = [&](int k, const Ctx::AirGroup& G, cudaStream_t st) -> int {
+      if (k == kStageFwdRows) {
+        if (ctx->fused_faces) {
+          const int n = G.f_hi - G.f_lo;
+          if (n > 0)
+            face2d_kernel<T><<<grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st>>>(buf, ctx->d_fwd2d + G.f_lo, n,
+                                                                                         ctx->f2d_smem);
+        } else {
+          xform_gemm_kernel<T><<<grid_for(ctx->fwd1.units, 1, gx), 256, 0, st>>>(
+              buf, ctx->d_fwd1, (int)ctx->fwd1.jobs.size(), ctx->fwd1.units);
+        }
+      } else if (k == kStageFwdCols) {
+        if (!ctx->fused_faces)
+          xform_gemm_kernel<T><<<grid_for(ctx->fwd2.units, 1, gx), 256, 0, st>>>(
+              buf, ctx->d_fwd2, (int)ctx->fwd2.jobs.size(), ctx->fwd2.units);
+      } else if (k == kStageModal) {
+        const int n = G.t_hi - G.t_lo;
+        if (n > 0) {
+          ModalArgs<T> ma{buf, ctx->d_dct, ctx->d_tiles + G.t_lo, n, ctx->d_srcpts, ctx->d_recpts,
+                          ctx->d_series, ctx->max_steps, ctx->d_t, tstep, par};
+          const int mgrid = grid_for(n, 1, ctx->num_sms * 2);
+          if (ctx->arith == ARD_ARITH_REFERENCE)
+            modal_kernel<T, true><<<mgrid, kModalThreads, msmem, st>>>(ma);
+          else
+            modal_kernel<T, false><<<mgrid, kModalThreads, msmem, st>>>(ma);
+        }
+      } else if (k == kStageRecorder) {
+        return launch_post_modal_range<T>(ctx, st, tstep, G.r_lo, G.r_hi, G.s_lo, G.s_hi, G.s_first, G.s_total);
+      } else if (k == kStageInvCols) {
+        if (ctx->fused_faces) {
+          const int n = G.i_hi - G.i_lo;
+          if (n > 0)
+            face2d_kernel<T><<<grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st>>>(buf, ctx->d_inv2d + G.i_lo, n,
+                                                                                         ctx->f2d_smem);
+        } else {
+          xform_gemm_kernel<T><<<grid_for(ctx->inv1.units, 1, gx), 256, 0, st>>>(
+              buf, ctx->d_inv1, (int)ctx->inv1.jobs.size(), ctx->inv1.units);
+        }
+      } else if (k == kStageInvRows) {
+        if (!ctx->fused_faces)
+          xform_gemm_kernel<T><<<grid_for(ctx->inv2.units, 1, gx), 256, 0, st>>>(
+              buf, ctx->d_inv2, (int)ctx->inv2.jobs.size(), ctx->inv2.units);
+      }
       ARD_CUDA(cudaGetLastError());
+      return ARD_OK;
+    };
+    const int stages[] = {kStageFwdRows, kStageFwdCols, kStageModal, kStageRecorder, kStageInvCols, kStageInvRows};
+    if (fork && ctx->ngroups == 2) {
+      // the second group's air branch on its own stream (independent until the interfaces)
+      ARD_CUDA(cudaStreamWaitEvent(ctx->stream3, ctx->ev_fork, 0));
+      for (int k : stages) {
+        if (int rc = stage(k, ctx->groups[0], s)) return rc;
+        if (int rc = stage(k, ctx->groups[1], ctx->stream3)) return rc;
+      }
+      ARD_CUDA(cudaEventRecord(ctx->ev_join3, ctx->stream3));
+      ARD_CUDA(cudaStreamWaitEvent(s, ctx->ev_join3, 0));
+    } else {
+      for (int k : stages) {
+        ARD_CUDA(mark(k));
+        for (int g = 0; g < ctx->ngroups; ++g)
+          if (int rc = stage(k, ctx->groups[g], s)) return rc;
+      }
     }
   }
   if (fork) {
@@ -390,19 +415,31 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   return ARD_OK;
 }
 
-// Recorder sums (with_recorders) and partial sums in one launch.
+// Recorder sums of recorders [r_lo, r_hi) and partial sums of jobs
+// [s_lo, s_hi) (their elements start at s_first, s_total of them) in one launch.
 template <typename T>
-int launch_post_modal(Ctx* ctx, cudaStream_t s, int tstep, bool with_recorders) {
-  const int nrec = with_recorders ? (int)ctx->recpts.size() : 0;
+int launch_post_modal_range(Ctx* ctx, cudaStream_t s, int tstep, int r_lo, int r_hi, int s_lo, int s_hi,
+                            long long s_first, long long s_total) {
+  const int nrec = r_hi - r_lo;
   const int rec_blocks = (nrec * 32 + 255) / 256;
-  const int sum_blocks = ctx->psum.empty() ? 0 : grid_for(ctx->psum_total, 256, ctx->num_sms * 8);
+  const int sum_blocks = s_total > 0 ? grid_for(s_total, 256, ctx->num_sms * 8) : 0;
   if (rec_blocks + sum_blocks == 0) return ARD_OK;
-  PostModalArgs<T> a{reinterpret_cast<T*>(ctx->d_buf), ctx->d_dct, ctx->d_recpts, nrec, ctx->d_hist, ctx->d_t,
-                     tstep, ctx->max_steps, rec_blocks, ctx->d_psum, (int)ctx->psum.size(),
-                     ctx->psum.empty() ? 0 : ctx->psum_total};
+  PostModalArgs<T> a{reinterpret_cast<T*>(ctx->d_buf), ctx->d_dct, ctx->d_recpts, r_lo, nrec, ctx->n_rec_total,
+                     ctx->d_hist, ctx->d_t, tstep, ctx->max_steps, rec_blocks, ctx->d_psum + s_lo, s_hi - s_lo,
+                     s_first, s_total};
   post_modal_kernel<T><<<rec_blocks + sum_blocks, 256, 0, s>>>(a);
   ARD_CUDA(cudaGetLastError());
   return ARD_OK;
+}
+
+template int launch_post_modal_range<float>(Ctx*, cudaStream_t, int, int, int, int, int, long long, long long);
+template int launch_post_modal_range<double>(Ctx*, cudaStream_t, int, int, int, int, int, long long, long long);
+
+// Recorder sums (with_recorders) and partial sums of all air partitions in one launch.
+template <typename T>
+int launch_post_modal(Ctx* ctx, cudaStream_t s, int tstep, bool with_recorders) {
+  return launch_post_modal_range<T>(ctx, s, tstep, 0, with_recorders ? (int)ctx->recpts.size() : 0, 0,
+                                    (int)ctx->psum.size(), 0, ctx->psum_total);
 }
 
 template int launch_post_modal<float>(Ctx*, cudaStream_t, int, bool);

@@ -62,6 +62,18 @@ struct Ctx {
   std::vector<Face2DJob> fwd2d, inv2d;      // fused face transforms
   std::vector<SumJob> psum;                 // partial sums before the inverse transforms
   long long psum_total = 0;
+  std::vector<int> psum_lo;                 // first partial-sum job of every air partition
+  // Air partitions in up to two groups whose air branches (face transforms,
+  // modal update, sums) run on two streams inside the step graph; ranges
+  // into the forward job lists, the tiles, the recorders and the sums.
+  struct AirGroup {
+    int part_lo = 0, part_hi = 0;
+    int f_lo = 0, f_hi = 0, i_lo = 0, i_hi = 0;
+    int t_lo = 0, t_hi = 0, r_lo = 0, r_hi = 0, s_lo = 0, s_hi = 0;
+    long long s_first = 0, s_total = 0;
+  };
+  int ngroups = 1;
+  AirGroup groups[2];
   bool fused_faces = false;
   Face2DSmem f2d_smem{0, 0, 0};
   size_t f2d_bytes = 0;
@@ -112,8 +124,8 @@ struct Ctx {
   long long* d_tb = nullptr;      // adjoint counters {current step, first step of the PML history}
   void* d_phist = nullptr;        // PmlHist<T> read by the PML kernel (adjoint contexts only)
 
-  cudaStream_t stream = nullptr, stream2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t stream = nullptr, stream2 = nullptr, stream3 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join3 = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   long long t_host = 0;
 };
@@ -131,6 +143,9 @@ int ensure_graph(Ctx* ctx);
 int check_guards(Ctx* ctx);
 template <typename T>
 int launch_post_modal(Ctx* ctx, cudaStream_t s, int tstep, bool with_recorders);
+template <typename T>
+int launch_post_modal_range(Ctx* ctx, cudaStream_t s, int tstep, int r_lo, int r_hi, int s_lo, int s_hi,
+                            long long s_first, long long s_total);
 void build_adjoint_jobs(Ctx* ctx);
 void pml_profile_unit(const Ctx* ctx, int type, int L, std::vector<double>* out);
 template <typename T>

@@ -241,15 +241,17 @@ template <typename T>
 struct PostModalArgs {
   T* buf;
   const DctDev* dct;
-  const PointDev* recs;
-  int nrec_total;
+  const PointDev* recs;   // all recorders; this launch takes [rec_first, rec_first + nrec)
+  int rec_first, nrec;
+  int nrec_total;         // row width of the history
   double* hist;
   const long long* tcount;
   int tstep;
   long long max_steps;
   int rec_blocks;
-  const SumJob* jobs;
+  const SumJob* jobs;     // this launch's sum jobs; their elements start at `first`
   int njobs;
+  long long first;
   long long total;
 };
 
@@ -257,8 +259,9 @@ template <typename T>
 __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
   if ((int)blockIdx.x < a.rec_blocks) {
     const int lane = threadIdx.x & 31;
-    const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (r >= a.nrec_total) return;
+    const int rl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (rl >= a.nrec) return;
+    const int r = a.rec_first + rl;
     const PointDev q = a.recs[r];
     const DctDev& D = a.dct[q.part];
     const int local_r = r - D.rec0;
@@ -274,13 +277,14 @@ __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
   const long long nb = (long long)gridDim.x - a.rec_blocks;
   for (long long g = ((long long)blockIdx.x - a.rec_blocks) * blockDim.x + threadIdx.x; g < a.total;
        g += nb * blockDim.x) {
+    const long long gg = g + a.first;   // element index among all sum jobs
     int lo = 0, hi = a.njobs - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (a.jobs[mid].first <= g) lo = mid; else hi = mid - 1;
+      if (a.jobs[mid].first <= gg) lo = mid; else hi = mid - 1;
     }
     const SumJob J = a.jobs[lo];
-    const T* p = buf + J.base + (g - J.first);
+    const T* p = buf + J.base + (gg - J.first);
     T v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int b = 0;
     for (; b + 8 <= J.nb; b += 8) {
@@ -290,7 +294,7 @@ __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
 #pragma unroll
     for (int k = 0; k < 7; ++k)
       if (b + k < J.nb) v[k] += p[(long long)(b + k) * J.stride];
-    buf[J.base + (g - J.first)] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+    buf[J.base + (gg - J.first)] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
   }
 }
 

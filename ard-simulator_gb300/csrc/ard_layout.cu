@@ -641,6 +641,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
 
   // ---- sums of the modal tiles' contraction partials (slab 0 receives the sum) ----
   for (const DctDev& D : ctx->dct) {
+    ctx->psum_lo.push_back((int)ctx->psum.size());
     const long long LX = 6LL * D.d * D.h, LY = 6LL * D.d * D.wp, LZ = 6LL * D.h * D.wp;
     const long long base[3] = {D.RX, D.RY, D.RZ}, cnt[3] = {LX, LY, LZ};
     const int nb[3] = {D.nbx, D.nby, D.nbz};
@@ -703,7 +704,8 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   {
     const size_t es0 = elem_size(ctx);
     long long xs = 0, x1 = 0, bs = 0, ts = 0;
-    for (const DctDev& D : ctx->dct) {
+    for (size_t pi = 0; pi < ctx->dct.size(); ++pi) {
+      const DctDev& D = ctx->dct[pi];
       struct Ax { long long f, p, P, R; int U, V, ld; long long cU, cV; };
       const Ax axes[3] = {{D.fX, D.pX, D.PX, D.RX, D.h, D.d, D.h, D.ch, D.cd},
                           {D.fY, D.pY, D.PY, D.RY, D.w, D.d, D.wp, D.cw, D.cd},
@@ -724,14 +726,14 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
             j.in0 = a.f + n * LS; j.in1 = a.f + (5 - n) * LS;
             j.out0 = a.P + n * LS; j.out1 = a.P + (3 + n) * LS;
             j.tabA = a.cV; j.tabB = a.cU + 2 * UU;
-            j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.sf;
+            j.V = a.V; j.U = a.U; j.ld = a.ld; j.u0 = u0; j.ub = ub; j.scale = D.sf; j.part = (int)pi;
             ctx->fwd2d.push_back(j);
             // inverse: even / odd parts (partials summed beforehand) -> layers n, 5-n
             Face2DJob k{};
             k.in0 = a.R + n * LS; k.in1 = a.R + (3 + n) * LS;
             k.out0 = a.p + n * LS; k.out1 = a.p + (5 - n) * LS;
             k.tabA = a.cV + 3 * VV; k.tabB = a.cU + UU;
-            k.V = a.V; k.U = a.U; k.ld = a.ld; k.u0 = u0; k.ub = ub; k.scale = D.si;
+            k.V = a.V; k.U = a.U; k.ld = a.ld; k.u0 = u0; k.ub = ub; k.scale = D.si; k.part = (int)pi;
             ctx->inv2d.push_back(k);
           }
         }
@@ -743,11 +745,67 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
                        ctx->f2d_bytes <= (size_t)std::min(ctx->smem_optin, 200 * 1024);
   }
   if (ctx->adjoint) build_adjoint_jobs(ctx);
+  // ---- air partition groups: two streams in the step graph when the fused
+  // face transforms are used and a split leaves each side >= 20 % of the cells ----
+  ctx->ngroups = 1;
+  {
+    const int np = (int)ctx->dct.size();
+    std::vector<long long> cells(np + 1, 0);
+    for (int i = 0; i < np; ++i) cells[i + 1] = cells[i] + (long long)ctx->dct[i].w * ctx->dct[i].h * ctx->dct[i].d;
+    int best = -1;
+    long long best_gap = cells[np];
+    for (int k = 1; k < np; ++k) {
+      const long long gap = std::llabs(cells[np] - 2 * cells[k]);
+      if (gap < best_gap) { best_gap = gap; best = k; }
+    }
+    if (ctx->fused_faces && best > 0 && std::min(cells[best], cells[np] - cells[best]) * 5 >= cells[np]) {
+      ctx->ngroups = 2;
+      ctx->groups[0].part_lo = 0; ctx->groups[0].part_hi = best;
+      ctx->groups[1].part_lo = best; ctx->groups[1].part_hi = np;
+    } else {
+      ctx->groups[0].part_lo = 0; ctx->groups[0].part_hi = np;
+    }
+    for (int g = 0; g < ctx->ngroups; ++g) {
+      Ctx::AirGroup& G = ctx->groups[g];
+      const int lo = G.part_lo, hi = G.part_hi;
+      G.t_lo = np ? ctx->dct[lo].tile0 : 0;
+      G.t_hi = hi < np ? ctx->dct[hi].tile0 : (int)ctx->tiles.size();
+      G.r_lo = np ? ctx->dct[lo].rec0 : 0;
+      G.r_hi = hi < np ? ctx->dct[hi].rec0 : (int)ctx->recpts.size();
+      G.s_lo = np ? ctx->psum_lo[lo] : 0;
+      G.s_hi = hi < np ? ctx->psum_lo[hi] : (int)ctx->psum.size();
+      G.s_first = G.s_lo < (int)ctx->psum.size() ? ctx->psum[G.s_lo].first : ctx->psum_total;
+      G.s_total = (G.s_hi < (int)ctx->psum.size() ? ctx->psum[G.s_hi].first : ctx->psum_total) - G.s_first;
+    }
+  }
   if (ctx->fused_faces) {
     const int per_sm = std::max(1, (int)(ctx->smem_per_sm / (ctx->f2d_bytes + 1024)));
     const int slots = ctx->num_sms * per_sm;
-    balance_face_jobs(&ctx->fwd2d, slots);
-    balance_face_jobs(&ctx->inv2d, slots);
+    // each group gets a share of one wave in proportion to its arithmetic
+    auto grouped = [&](std::vector<Face2DJob>* list, auto set_range) {
+      if (ctx->ngroups == 1) {
+        balance_face_jobs(list, slots);
+        set_range(0, 0, (int)list->size());
+        return;
+      }
+      std::vector<Face2DJob> parts[2];
+      double w[2] = {0, 0};
+      for (const Face2DJob& j : *list) {
+        const int g = j.part >= ctx->groups[1].part_lo ? 1 : 0;
+        parts[g].push_back(j);
+        w[g] += (double)j.V * (j.U + j.V) * j.ub;
+      }
+      list->clear();
+      for (int g = 0; g < 2; ++g) {
+        const int sg = std::max(1, (int)std::lround(slots * w[g] / std::max(1.0, w[0] + w[1])));
+        balance_face_jobs(&parts[g], sg);
+        const int lo = (int)list->size();
+        list->insert(list->end(), parts[g].begin(), parts[g].end());
+        set_range(g, lo, (int)list->size());
+      }
+    };
+    grouped(&ctx->fwd2d, [&](int g, int lo, int hi) { ctx->groups[g].f_lo = lo; ctx->groups[g].f_hi = hi; });
+    grouped(&ctx->inv2d, [&](int g, int lo, int hi) { ctx->groups[g].i_lo = lo; ctx->groups[g].i_hi = hi; });
     balance_face_jobs(&ctx->adj1_2d, slots);
     balance_face_jobs(&ctx->adj2_2d, slots);
   }
@@ -757,6 +815,8 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   ctx->pool_elems = pool.off;
   ARD_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   ARD_CUDA(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
+  ARD_CUDA(cudaStreamCreateWithFlags(&ctx->stream3, cudaStreamNonBlocking));
+  ARD_CUDA(cudaEventCreateWithFlags(&ctx->ev_join3, cudaEventDisableTiming));
   ARD_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
   ARD_CUDA(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
   // checked mode: 16 MiB sentinel guards on both sides of the pool catch stray writes
@@ -856,6 +916,8 @@ void free_ctx_device(Ctx* ctx) {
     if (p) cudaFree(p);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->ev_join3) cudaEventDestroy(ctx->ev_join3);
+  if (ctx->stream3) cudaStreamDestroy(ctx->stream3);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
   ctx->graph_exec = nullptr;
