@@ -303,9 +303,16 @@ constexpr int kFace2DThreads = 512;
 struct Face2DSmem {
   int xs;  // X0 and later A: max(V * xp, V * ap)
   int x1;  // X1: V * xp
-  int bs;  // B slab: roundup(U, 4) * 33
-  int ts;  // each of T0, T1: V * 33
+  int bs;  // B slab, column-major: 32 * face2d_pitch(U)
+  int ts;  // each of T0, T1, column-major: 32 * face2d_pitch(V)
 };
+
+// Column pitch of the column-major slab arrays: 4 mod 8 elements, so the 128-bit
+// loads of a quarter warp (8 columns) hit distinct bank groups.
+__host__ __device__ inline int face2d_pitch(int n) {
+  const int n4 = (n + 3) & ~3;
+  return n4 + ((n4 & 7) ? 8 : 4);
+}
 
 // One block per (layer pair, 32-column slab): X0, X1 (V x U, row pitch ld)
 // are staged in shared memory with cp.async, combined into E = X0 + X1 and
@@ -360,10 +367,11 @@ __global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ 
       }
     }
     const T* B = buf + J.tabB;
+    const int pb = face2d_pitch(U), pt = face2d_pitch(V);
     for (int i = tid; i < Up * 32; i += kFace2DThreads) {
       const int j = i >> 5, c = i & 31;
       const bool ok = j < U && c < J.ub;
-      cp_async_scalar(Bs + j * 33 + c, B + (ok ? (long long)j * U + J.u0 + c : 0), ok);
+      cp_async_scalar(Bs + c * pb + j, B + (ok ? (long long)j * U + J.u0 + c : 0), ok);
     }
     cp_async_commit();
     cp_async_wait<0>();
@@ -390,8 +398,9 @@ __global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ 
 #pragma unroll
         for (int i = 0; i < 4; ++i) rr[i] = min(r0 + rstr * i, V - 1);
         for (int j = 0; j < U; j += 4) {
-          const T b0 = Bs[j * 33 + col], b1 = Bs[(j + 1) * 33 + col];
-          const T b2 = Bs[(j + 2) * 33 + col], b3 = Bs[(j + 3) * 33 + col];
+          T bq[4];
+          load4(Bs + col * pb + j, bq);
+          const T b0 = bq[0], b1 = bq[1], b2 = bq[2], b3 = bq[3];
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             T x[4], y[4];
@@ -408,14 +417,22 @@ __global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ 
 #pragma unroll
         for (int i = 0; i < 4; ++i)
           if (r0 + rstr * i < V) {
-            if constexpr (DE) T0[(r0 + rstr * i) * 33 + col] = e[i];
-            if constexpr (DO) T1[(r0 + rstr * i) * 33 + col] = o[i];
+            if constexpr (DE) T0[col * pt + r0 + rstr * i] = e[i];
+            if constexpr (DO) T1[col * pt + r0 + rstr * i] = o[i];
           }
       }
     };
     if (J.which == 0) along_u(std::true_type{}, std::true_type{});
     else if (J.which == 1) along_u(std::true_type{}, std::false_type{});
     else along_u(std::false_type{}, std::true_type{});
+    {  // rows V .. roundup(V, 4) - 1 of T read as zero
+      const int vt = ((V + 3) & ~3) - V;
+      for (int i = tid; i < 32 * vt; i += kFace2DThreads) {
+        const int c = i / vt, r = V + i - c * vt;
+        T0[c * pt + r] = (T)0;
+        T1[c * pt + r] = (T)0;
+      }
+    }
     __syncthreads();
     // ---- A (V x V, row o contiguous) into the X0 area (asynchronous) ----
     const T* A = buf + J.tabA;
@@ -447,12 +464,8 @@ __global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ 
         for (int i = 0; i < 4; ++i) oo[i] = min(o0 + rstr * i, V - 1);
         for (int r = 0; r < V; r += 4) {
           T t[4], u[4];
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const bool ok = r + k < V;
-            if constexpr (DE) t[k] = ok ? T0[(r + k) * 33 + col] : (T)0;
-            if constexpr (DO) u[k] = ok ? T1[(r + k) * 33 + col] : (T)0;
-          }
+          if constexpr (DE) load4(T0 + col * pt + r, t);
+          if constexpr (DO) load4(T1 + col * pt + r, u);
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             T a4[4];

@@ -716,8 +716,8 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         const long long xp = ((a.U + 3) & ~3) + 4, ap = ((a.V + 3) & ~3) + 4;
         xs = std::max(xs, std::max((long long)a.V * xp, (long long)a.V * ap));
         x1 = std::max(x1, (long long)a.V * xp);
-        bs = std::max(bs, (long long)((a.U + 3) & ~3) * 33);
-        ts = std::max(ts, (long long)a.V * 33);
+        bs = std::max(bs, 32LL * face2d_pitch(a.U));
+        ts = std::max(ts, 32LL * face2d_pitch(a.V));
         for (int u0 = 0; u0 < a.U; u0 += 32) {
           const int ub = std::min(32, a.U - u0);
           for (int n = 0; n < 3; ++n) {
