@@ -263,3 +263,33 @@ def test_write_outputs_in_reference_format(tmp_path):
         np.testing.assert_allclose(vals, rec[:, r], rtol=1e-5, atol=1e-30)
     src = np.loadtxt(tmp_path / "source_0.txt")
     np.testing.assert_allclose(src, g["sources"][0][:T], rtol=1e-5)
+
+
+def test_edge_cases_empty_and_ragged():
+    """Zero-step runs, a scene without sources or recorders, odd extents
+    (not multiples of 4 or 8), steps past max_steps (no history, no source)."""
+    dh, c0 = 0.1, 343.0
+    dt = 0.5 * dh / (c0 * np.sqrt(3.0))
+    # no sources, no recorders: the state stays exactly zero
+    sim = A.Simulation(A.build_scene([(0, 0, 0, 13, 11, 9)], [], [], dh, dt, c0, 5), max_steps=16)
+    sim.run(0)
+    assert sim.time_step == 0
+    sim.run(20)                                   # past max_steps: stepping continues
+    assert sim.time_step == 20
+    assert np.all(sim.field(0) == 0)
+    # ragged extents with a source and recorders; FP32 against the FP64 C oracle
+    air, srcs, recs = [(0, 0, 0, 17, 13, 15), (17, 1, 0, 11, 12, 15)], [(5, 6, 7)], [(8, 6, 7), (23, 7, 7)]
+    T = 40
+    series = (np.hanning(T) * 1e3).astype(np.float32)
+    flat = O.make_flat_scene(air, srcs, recs, dict(dh=dh, dt=float(np.float32(dt)), c0=c0, pml_layers=5))
+    ref = O.OracleSim(flat, "f64")
+    ref.set_source_series(0, series)
+    ref.step(T)
+    want = ref.recorders()
+    sim = A.Simulation(A.build_scene(air, srcs, recs, dh, float(np.float32(dt)), c0, 5), max_steps=T)
+    sim.set_source_series(0, series)
+    sim.run(T)
+    got = sim.recorders(f64=True)
+    for r in range(want.shape[1]):
+        if np.abs(want[:, r]).max() > 0:
+            assert rel_l2(got[:, r], want[:, r]) < F32_TOL, r
