@@ -122,10 +122,28 @@ __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, co
   constexpr int NR = BK / 4;                     // elements of each operand a thread stages per chunk
   __shared__ __align__(16) T Ps[2][BK][64 + 4];  // P(m0 + mm, k0 + kk) at [kk][mm]
   __shared__ __align__(16) T Qs[2][BK][64 + 4];  // Q(k0 + kk, n0 + nn) at [kk][nn]
+  // first unit of every job, cached in shared memory for the per-unit job search
+  constexpr int kMaxCachedJobs = 1024;
+  __shared__ int sfirst[kMaxCachedJobs];
   const int tid = threadIdx.x;
   const int ty = tid >> 4, tx = tid & 15;
+  const bool cached = njobs <= kMaxCachedJobs;
+  if (cached)
+    for (int i = tid; i < njobs; i += 256) sfirst[i] = jobs[i].first;
+  __syncthreads();
   for (int unit = blockIdx.x; unit < total; unit += gridDim.x) {
-    const XformJob J = jobs[find_job(jobs, njobs, unit)];
+    int ji;
+    if (cached) {
+      int lo = 0, hi = njobs - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sfirst[mid] <= unit) lo = mid; else hi = mid - 1;
+      }
+      ji = lo;
+    } else {
+      ji = find_job(jobs, njobs, unit);
+    }
+    const XformJob J = jobs[ji];
     const int t = unit - J.first;
     const int m0 = (t / J.tn) * 64, n0 = (t % J.tn) * 64;
     const int Md = J.rows ? J.batch : J.n;
@@ -204,14 +222,19 @@ __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, co
       sb ^= 1;
     }
     const T scale = (T)J.scale;
+    const int nb = n0 + tx * 4;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int m = m0 + ty * 4 + i;
       if (m >= Md) continue;
+      const long long o = J.out + (long long)m * J.ld + nb;
+      if (nb + 3 < Nd && (o & 3) == 0) {
+        T v[4] = {acc[i][0] * scale, acc[i][1] * scale, acc[i][2] * scale, acc[i][3] * scale};
+        store4(buf + o, v);
+      } else {
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int n = n0 + tx * 4 + j;
-        if (n < Nd) buf[J.out + (long long)m * J.ld + n] = acc[i][j] * scale;
+        for (int j = 0; j < 4; ++j)
+          if (nb + j < Nd) buf[o + j] = acc[i][j] * scale;
       }
     }
   }
