@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -48,11 +49,12 @@ struct AdjBuffers {
   void* resid = nullptr;      // [T][n_rec_total] residuals (context precision)
   double* gsrc = nullptr;     // [T][n_src_total]
   double* gz = nullptr;       // [pml blocks][kMaxPmlLayers]
-  void* ckpt = nullptr;       // [n_ckpt + 1][state] (last: the state after step T)
+  void* ckpt = nullptr;       // [n_ckpt + 1][state or PML state] (last: after step T)
   void* hist_p = nullptr;     // [K + 1][region]
   void* hist_phn = nullptr;   // [K][region]
+  void* fhist = nullptr;      // [T][strip region] (PML replay)
   ~AdjBuffers() {
-    void* ptrs[] = {resid, gsrc, gz, ckpt, hist_p, hist_phn};
+    void* ptrs[] = {resid, gsrc, gz, ckpt, hist_p, hist_phn, fhist};
     for (void* p : ptrs)
       if (p) cudaFree(p);
   }
@@ -241,34 +243,65 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
   const bool need_hist = grad_scale != nullptr && !ctx->pml.empty();
   const long long state_len = ctx->state_end - ctx->state_begin;
   const long long hlen = ctx->pml_region[0][1] - ctx->pml_region[0][0];
+  // How the forward PML values reach the backward sweep (damping gradient only):
+  //   kFull     the whole history p(t), phi_n(t) kept in one forward run
+  //   kReplay   the strip forcing of every step and a copy of the PML state every
+  //             K steps are kept; each segment's PML runs again on its own
+  //   kRecompute  a copy of the whole state every K steps; each segment runs again
+  enum { kNone, kFull, kReplay, kRecompute } mode = kNone;
   long long K = T_steps, n_ckpt = 1;
-  bool use_ckpt = false;
+  const long long pml_begin = ctx->pml_region[0][0];
+  const long long pml_len = ctx->state_end - pml_begin;       // PML fields + strip forces
+  const long long flen = ctx->state_end - ctx->force_begin;    // strip forces
   AdjBuffers ab;
   if (need_hist) {
     size_t free_b = 0, total_b = 0;
     ARD_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t budget = free_b / 10 * 9;
     const size_t full = (size_t)(2 * T_steps + 1) * hlen * es;
-    if (checkpoint_every > 0) {
-      K = std::min<long long>(checkpoint_every, T_steps);
-      use_ckpt = true;
-    } else if (full > free_b / 2) {
-      // balance checkpoint memory (n_ckpt states) against history memory (2 K PML regions)
-      const double k = std::sqrt((double)T_steps * (double)state_len / (2.0 * (double)std::max(1LL, hlen)));
-      K = std::max(1LL, std::min(T_steps, (long long)std::ceil(k)));
-      use_ckpt = true;
+    auto segment_k = [&](long long ckpt_len) {
+      // balance checkpoint memory (n_ckpt copies) against history memory (2 K PML regions)
+      const double k = std::sqrt((double)T_steps * (double)ckpt_len / (2.0 * (double)std::max(1LL, hlen)));
+      return std::max(1LL, std::min(T_steps, (long long)std::ceil(k)));
+    };
+    // ARD_ADJOINT_RECOMPUTE=1 (tests): the segment-recompute path even where the replay fits
+    const char* force_rc = std::getenv("ARD_ADJOINT_RECOMPUTE");
+    const bool recompute_only = force_rc && force_rc[0] == '1';
+    if (checkpoint_every <= 0 && full <= free_b / 2 && !recompute_only) {
+      mode = kFull;
+    } else {
+      K = checkpoint_every > 0 ? std::min<long long>(checkpoint_every, T_steps) : segment_k(pml_len);
+      n_ckpt = (T_steps + K - 1) / K;
+      const size_t replay = ((size_t)T_steps * flen + (size_t)(n_ckpt + 1) * pml_len + (size_t)(2 * K + 1) * hlen) * es;
+      if (replay <= budget && !recompute_only) {
+        mode = kReplay;
+      } else {
+        if (checkpoint_every <= 0) K = segment_k(state_len);
+        n_ckpt = (T_steps + K - 1) / K;
+        mode = kRecompute;
+      }
     }
-    n_ckpt = (T_steps + K - 1) / K;
-    const size_t need = (use_ckpt ? (size_t)(n_ckpt + 1) * state_len * es : 0) + (size_t)(2 * K + 1) * hlen * es;
-    if (need > free_b / 10 * 9) {
+    if (mode != kFull) n_ckpt = (T_steps + K - 1) / K;
+    size_t need = (size_t)(2 * K + 1) * hlen * es;
+    if (mode == kReplay) need += ((size_t)T_steps * flen + (size_t)(n_ckpt + 1) * pml_len) * es;
+    if (mode == kRecompute) need += (size_t)(n_ckpt + 1) * state_len * es;
+    if (need > budget) {
       ctx->err = "ard_adjoint: checkpoints and PML history need " + std::to_string(need >> 20) + " MiB (" +
                  std::to_string(n_ckpt) + " checkpoints every " + std::to_string(K) + " steps); " +
                  std::to_string(free_b >> 20) + " MiB free";
       return ARD_ERR_OOM;
     }
-    if (use_ckpt) ARD_CUDA(cudaMalloc(&ab.ckpt, (size_t)(n_ckpt + 1) * state_len * es));
+    if (mode == kReplay) {
+      ARD_CUDA(cudaMalloc(&ab.ckpt, (size_t)(n_ckpt + 1) * pml_len * es));
+      ARD_CUDA(cudaMalloc(&ab.fhist, std::max<size_t>(1, (size_t)T_steps * flen * es)));
+    }
+    if (mode == kRecompute) ARD_CUDA(cudaMalloc(&ab.ckpt, (size_t)(n_ckpt + 1) * state_len * es));
     ARD_CUDA(cudaMalloc(&ab.hist_p, (size_t)(K + 1) * hlen * es));
     ARD_CUDA(cudaMalloc(&ab.hist_phn, (size_t)K * hlen * es));
   }
+  ctx->adj_mode = mode == kFull ? "whole PML history" : mode == kReplay ? "PML replay" :
+                  mode == kRecompute ? "segment recompute" : "no forward values";
+  ctx->adj_k = mode == kReplay || mode == kRecompute ? K : 0;
   const int nrec = ctx->n_rec_total, nsrc = ctx->n_src_total;
   ARD_CUDA(cudaMalloc(&ab.resid, std::max<size_t>(1, (size_t)T_steps * nrec * es)));
   ARD_CUDA(cudaMalloc(&ab.gsrc, std::max<size_t>(1, (size_t)T_steps * nsrc * sizeof(double))));
@@ -278,39 +311,48 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
 
   T* buf = reinterpret_cast<T*>(ctx->d_buf);
   T* state = buf + ctx->state_begin;
-  auto ckpt = [&](long long i) { return reinterpret_cast<T*>(ab.ckpt) + i * state_len; };
+  T* pml_state = buf + pml_begin;
+  const long long ckpt_len = mode == kReplay ? pml_len : state_len;
+  T* ckpt_src = mode == kReplay ? pml_state : state;
+  auto ckpt = [&](long long i) { return reinterpret_cast<T*>(ab.ckpt) + i * ckpt_len; };
 
-  // The PML kernel keeps p(t) and phi_n(t) of steps t0 <= t < t1 (the slot
-  // of p(t0 - 1) is filled here from the state before step t0).
+  // What the PML kernel records or replays (PmlHist): p(t), phi_n(t) of
+  // steps t0 <= t < t1 (the slot of p(t0 - 1) filled here from the state
+  // before step t0), the strip forcing of steps [ft0, ft1), and the forcing
+  // it replays.
   T* hp = reinterpret_cast<T*>(ab.hist_p);
   T* hphn = reinterpret_cast<T*>(ab.hist_phn);
-  auto keep_history = [&](long long t0, long long t1) -> int {
-    PmlHist<T> h{hp, hphn, hlen, t0, t1};
-    const int q_prev = (int)((t0 + 1) & 1);   // level of p(t0 - 1)
-    ARD_CUDA(cudaMemcpyAsync(hp, buf + ctx->pml_region[q_prev][0], hlen * es, cudaMemcpyDeviceToDevice, s));
-    ARD_CUDA(cudaMemcpyAsync(ctx->d_phist, &h, sizeof(h), cudaMemcpyHostToDevice, s));
-    return ARD_OK;
-  };
-  auto stop_history = [&]() -> int {
-    PmlHist<T> h{nullptr, nullptr, 0, 0, 0};
+  T* fh = reinterpret_cast<T*>(ab.fhist);
+  auto set_hist = [&](bool keep, long long t0, long long t1, bool rec_force, bool replay) -> int {
+    PmlHist<T> h{};
+    if (keep) {
+      h.p = hp; h.phn = hphn; h.hlen = hlen; h.t0 = t0; h.t1 = t1;
+      const int q_prev = (int)((t0 + 1) & 1);   // level of p(t0 - 1)
+      ARD_CUDA(cudaMemcpyAsync(hp, buf + ctx->pml_region[q_prev][0], hlen * es, cudaMemcpyDeviceToDevice, s));
+    }
+    h.flen = flen;
+    if (rec_force) { h.f = fh; h.ft0 = 0; h.ft1 = T_steps; }
+    if (replay) { h.fsrc = fh; h.fs0 = 0; }
     ARD_CUDA(cudaMemcpyAsync(ctx->d_phist, &h, sizeof(h), cudaMemcpyHostToDevice, s));
     return ARD_OK;
   };
 
-  // ---- forward run: keeps the whole PML history, or a checkpoint at the start of every segment ----
+  // ---- forward run ----
   ard_ctx* handle = reinterpret_cast<ard_ctx*>(ctx);
-  if (use_ckpt) {
+  if (mode == kReplay || mode == kRecompute) {
+    if (mode == kReplay && (rc = set_hist(false, 0, 0, true, false))) return rc;
     for (long long i = 0; i < n_ckpt; ++i) {
-      ARD_CUDA(cudaMemcpyAsync(ckpt(i), state, state_len * es, cudaMemcpyDeviceToDevice, s));
+      ARD_CUDA(cudaMemcpyAsync(ckpt(i), ckpt_src, ckpt_len * es, cudaMemcpyDeviceToDevice, s));
       rc = ard_step(handle, std::min(K, T_steps - i * K), nullptr);
       if (rc) return rc;
     }
-    ARD_CUDA(cudaMemcpyAsync(ckpt(n_ckpt), state, state_len * es, cudaMemcpyDeviceToDevice, s));
+    ARD_CUDA(cudaMemcpyAsync(ckpt(n_ckpt), ckpt_src, ckpt_len * es, cudaMemcpyDeviceToDevice, s));
+    if ((rc = set_hist(false, 0, 0, false, false))) return rc;
   } else {
-    if (need_hist && (rc = keep_history(0, T_steps))) return rc;
+    if (mode == kFull && (rc = set_hist(true, 0, T_steps, false, false))) return rc;
     rc = ard_step(handle, T_steps, nullptr);
     if (rc) return rc;
-    if (need_hist && (rc = stop_history())) return rc;
+    if (mode == kFull && (rc = set_hist(false, 0, 0, false, false))) return rc;
   }
 
   // ---- residuals and misfit ----
@@ -340,23 +382,29 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
   ARD_CUDA(cudaMemsetAsync(buf + ctx->adj_begin, 0, adj_len * es, s));
   const HistView hv = need_hist ? HistView{ab.hist_p, ab.hist_phn, hlen, ab.gz} : HistView{};
   AdjGraph graph;   // captured on first use, for this call's buffers
-  if (use_ckpt) {
+  if (mode == kReplay || mode == kRecompute) {
     for (long long i = n_ckpt - 1; i >= 0; --i) {
       const long long t0 = i * K, t1 = std::min(T_steps, t0 + K);
       // run the segment again from its checkpoint, keeping its PML history
-      ARD_CUDA(cudaMemcpyAsync(state, ckpt(i), state_len * es, cudaMemcpyDeviceToDevice, s));
+      ARD_CUDA(cudaMemcpyAsync(ckpt_src, ckpt(i), ckpt_len * es, cudaMemcpyDeviceToDevice, s));
       set_step_counter_kernel<<<1, 32, 0, s>>>(ctx->d_t, t0);
       ARD_CUDA(cudaGetLastError());
-      ctx->t_host = t0;
-      if ((rc = keep_history(t0, t1))) return rc;
-      rc = ard_step(handle, t1 - t0, nullptr);
-      if (rc) return rc;
-      if ((rc = stop_history())) return rc;
+      if ((rc = set_hist(true, t0, t1, false, mode == kReplay))) return rc;
+      if (mode == kReplay) {
+        // the PML on its own, driven by the recorded strip forcing
+        for (long long t = t0; t < t1; ++t)
+          if ((rc = launch_pml<T>(ctx, (int)(t & 1), (int)(t - t0), s))) return rc;
+      } else {
+        ctx->t_host = t0;
+        rc = ard_step(handle, t1 - t0, nullptr);
+        if (rc) return rc;
+      }
+      if ((rc = set_hist(false, 0, 0, false, false))) return rc;
       rc = run_backward<T>(ctx, t1, t0, t0, ab, hv, &graph);
       if (rc) return rc;
     }
     // leave the forward state as after step T
-    ARD_CUDA(cudaMemcpyAsync(state, ckpt(n_ckpt), state_len * es, cudaMemcpyDeviceToDevice, s));
+    ARD_CUDA(cudaMemcpyAsync(ckpt_src, ckpt(n_ckpt), ckpt_len * es, cudaMemcpyDeviceToDevice, s));
     set_step_counter_kernel<<<1, 32, 0, s>>>(ctx->d_t, T_steps);
     ARD_CUDA(cudaGetLastError());
     ctx->t_host = T_steps;

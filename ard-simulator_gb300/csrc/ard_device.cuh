@@ -89,6 +89,7 @@ struct PmlDev {
   long long zeta;         // [L] damping profile (scaled)
   long long n;            // L*A*B
   long long hoff;         // offset of the slab inside each all-slab region (p, phi: same for all eight)
+  long long foff;         // offset of the slab's strip force inside the all-slab strip region
 };
 
 // Side of an interface: an air partition's face layers or a PML slab, both

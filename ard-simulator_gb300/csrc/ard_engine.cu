@@ -235,7 +235,10 @@ extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_o
 
 extern "C" int ard_describe(const ard_ctx* c, char* buf, int64_t n) {
   if (!c || !buf || n < 1) return ARD_ERR_INVALID;
-  const std::string& e = reinterpret_cast<const Ctx*>(c)->tuning;
+  const Ctx* ctx = reinterpret_cast<const Ctx*>(c);
+  std::string e = ctx->tuning;
+  if (!ctx->adj_mode.empty())
+    e += "; last adjoint: " + ctx->adj_mode + (ctx->adj_k ? ", segments of " + std::to_string(ctx->adj_k) + " steps" : "");
   const size_t k = std::min<size_t>((size_t)(n - 1), e.size());
   std::memcpy(buf, e.data(), k);
   buf[k] = 0;
@@ -326,12 +329,7 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   }
   cudaStream_t sp = fork ? s2 : s;
   ARD_CUDA(mark(kStagePml));
-  if (!ctx->pml_blocks.empty()) {
-    PmlArgs<T> pa{buf, ctx->d_pml, ctx->d_pml_blocks, (int)ctx->pml_blocks.size(), par,
-                  (T)ctx->dt, (T)ctx->dh, (T)ctx->c0, (const PmlHist<T>*)ctx->d_phist, ctx->d_t, tstep};
-    pml_kernel<T><<<grid_for((long long)ctx->pml_blocks.size(), 1, ctx->num_sms * 8), 256, 0, sp>>>(pa);
-    ARD_CUDA(cudaGetLastError());
-  }
+  if (int rc = launch_pml<T>(ctx, par, tstep, sp)) return rc;
   if (!ctx->dct.empty()) {
     const int gx = ctx->num_sms * 4;
     const size_t msmem = kModalSmemElems * sizeof(T);
@@ -414,6 +412,20 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   ARD_CUDA(mark(kNumStages));
   return ARD_OK;
 }
+
+// The PML update of every slab for step (*d_t + tstep).
+template <typename T>
+int launch_pml(Ctx* ctx, int par, int tstep, cudaStream_t s) {
+  if (ctx->pml_blocks.empty()) return ARD_OK;
+  PmlArgs<T> pa{reinterpret_cast<T*>(ctx->d_buf), ctx->d_pml, ctx->d_pml_blocks, (int)ctx->pml_blocks.size(), par,
+                (T)ctx->dt, (T)ctx->dh, (T)ctx->c0, (const PmlHist<T>*)ctx->d_phist, ctx->d_t, tstep};
+  pml_kernel<T><<<grid_for((long long)ctx->pml_blocks.size(), 1, ctx->num_sms * 8), 256, 0, s>>>(pa);
+  ARD_CUDA(cudaGetLastError());
+  return ARD_OK;
+}
+
+template int launch_pml<float>(Ctx*, int, int, cudaStream_t);
+template int launch_pml<double>(Ctx*, int, int, cudaStream_t);
 
 // Recorder sums of recorders [r_lo, r_hi) and partial sums of jobs
 // [s_lo, s_hi) (their elements start at s_first, s_total of them) in one launch.

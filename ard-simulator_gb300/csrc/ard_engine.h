@@ -87,6 +87,7 @@ struct Ctx {
   long long state_begin = 0, state_end = 0;  // checkpointed state block
   long long adj_begin = 0, adj_end = 0;      // adjoint state block
   long long pml_region[8][2] = {};           // all slabs' p0, p1, phn0, phn1, pha0, pha1, phb0, phb1
+  long long force_begin = 0;                 // all slabs' strip forces: [force_begin, state_end)
   bool adjoint = false;
   // layout choices (the autotuner varies them; defaults are the heuristics)
   int tune_tiles = 1;      // modal tiles per wave slot (x 2 per SM): kz split finer when > 1
@@ -99,6 +100,8 @@ struct Ctx {
   JobList adjg[4];
   long long q_begin = 0, q_end = 0;          // adjoint face pressure (zeroed every adjoint step)
   bool adj_valid = false;                    // adjoint levels hold mu(0), mu(1) of the last ard_adjoint
+  std::string adj_mode;                      // how the last ard_adjoint obtained forward PML values
+  long long adj_k = 0;                       // its segment length
 
   // device memory
   void* d_buf = nullptr;          // element pool (float or double)
@@ -139,6 +142,8 @@ void free_ctx_device(Ctx* ctx);
 template <typename T>
 int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, bool fork, cudaEvent_t* ev);
 int launch_steps_direct(Ctx* ctx, int n, cudaStream_t s);
+template <typename T>
+int launch_pml(Ctx* ctx, int par, int tstep, cudaStream_t s);
 int ensure_graph(Ctx* ctx);
 int check_guards(Ctx* ctx);
 template <typename T>

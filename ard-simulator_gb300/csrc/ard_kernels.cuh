@@ -896,12 +896,22 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
 // t0 <= t < t1 the PML kernel also writes p(t) to p[(t - t0 + 1) hlen + ...]
 // and phi_n(t) to phn[(t - t0) hlen + ...] (all-slab region layout, slab at
 // PmlDev::hoff).  p == null: nothing is kept.
+// Strip forces: for steps ft0 <= t < ft1 the kernel also writes the strip
+// force it reads (the interfaces' forcing of step t-1) to f[(t - ft0) flen +
+// PmlDev::foff + ...]; with fsrc set it reads the strip force of step t from
+// fsrc[(t - fs0) flen + ...] instead of the context's strips (the PML runs
+// again on its own, replaying the recorded forcing).
 template <typename T>
 struct PmlHist {
   T* p;
   T* phn;
   long long hlen;
   long long t0, t1;
+  T* f;
+  long long flen;
+  long long ft0, ft1;
+  const T* fsrc;
+  long long fs0;
 };
 
 template <typename T>
@@ -935,6 +945,8 @@ __global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
   const int tb = threadIdx.x & 31, ta = threadIdx.x >> 5;
   T* hp = nullptr;
   T* hfn = nullptr;
+  T* hf = nullptr;
+  const T* fsrc = nullptr;
   if (a.hist) {
     const PmlHist<T> h = *a.hist;
     const long long t = *a.tcount + a.tstep;
@@ -942,6 +954,8 @@ __global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
       hp = h.p + (t - h.t0 + 1) * h.hlen;
       hfn = h.phn + (t - h.t0) * h.hlen;
     }
+    if (h.f && t >= h.ft0 && t < h.ft1) hf = h.f + (t - h.ft0) * h.flen;
+    if (h.fsrc) fsrc = h.fsrc + (t - h.fs0) * h.flen;
   }
   for (int bi = blockIdx.x; bi < a.nblocks; bi += gridDim.x) {
     const int4 blk = a.blocks[bi];
@@ -961,7 +975,8 @@ __global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
     T* fa_o = a.buf + P.pha[a.par];
     T* fb_o = a.buf + P.phb[a.par];
     const T* zeta = a.buf + P.zeta;
-    const T* force = a.buf + P.force;
+    const T* force = fsrc ? fsrc + P.foff : a.buf + P.force;
+    T* force_rec = hf ? hf + P.foff : nullptr;
     // register windows along the normal: p(l-3 .. l+3), phi_n(l-2 .. l+2)
     T pw[7], fw[5];
 #pragma unroll
@@ -1031,6 +1046,10 @@ __global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
       const T pold = nold, f = nforce;
       if (l + 1 < L) fetch(l + 1);
       __syncthreads();
+      if (force_rec && inside) {
+        const int sl = l - P.strip0;
+        if (sl >= 0 && sl < 3) force_rec[sl * lstride + col] = f;
+      }
       if (inside) {
         T ln = 0, la = 0, lb = 0;
 #pragma unroll

@@ -414,7 +414,11 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     }
     ctx->pml_region[q][1] = pool.off;
   }
-  for (PmlDev& P : ctx->pml) P.force = pool.take(3LL * P.A * P.B);
+  ctx->force_begin = pool.off;
+  for (PmlDev& P : ctx->pml) {
+    P.force = pool.take(3LL * P.A * P.B);
+    P.foff = P.force - ctx->force_begin;
+  }
   ctx->state_end = pool.off;
   // a slab sits at the same offset inside each of the eight regions
   for (PmlDev& P : ctx->pml) {

@@ -278,10 +278,15 @@ int ard_read_field_noalloc(ard_ctx* ctx, int32_t scene, int32_t partition, float
  *                ard_set_source_series)          dJ/d(source series)
  *   grad_scale   6 floats per scene, ARD_PML_*   dJ/d(PML face scale)
  *   loss         1 float per scene
- * grad_scale needs forward PML values in reverse order: the forward run
- * then keeps a copy of the state every `checkpoint_every` steps (<= 0:
- * chosen to balance checkpoint and history memory) and each segment is run
- * again before its backward sweep.  Without grad_scale nothing is stored.
+ * grad_scale needs forward PML values in reverse order.  With
+ * checkpoint_every <= 0 the whole PML history is kept when it fits in half
+ * the free device memory.  Otherwise (or with checkpoint_every > 0) the
+ * forward run keeps the interfaces' forcing of the PML strips for every step
+ * and a copy of the PML state every K steps (K = checkpoint_every, or chosen
+ * to balance the memories), and each segment's PML runs again on its own
+ * before its backward sweep; where even that does not fit, a copy of the
+ * whole state every K steps and the whole segment runs again.  Without
+ * grad_scale nothing is stored.  ard_describe names the path taken.
  * dJ/d(initial pressure) of an air partition is read afterwards with
  * ard_read_initial_pressure_grad (width*height*depth floats, [z][y][x]). */
 int ard_adjoint(ard_ctx* ctx, int64_t T, const float* target,

@@ -130,11 +130,19 @@ def test_pml_scale_gradient(problem):
         assert abs(g[f] - fd) <= 2e-5 * np.abs(g).max(), (f, g[f], fd)
 
 
-def test_checkpoint_interval_does_not_change_gradients(problem):
-    for K in (0, 7, T_STEPS):   # 0: the whole PML history kept in one forward run
+def test_checkpoint_interval_does_not_change_gradients(problem, monkeypatch):
+    for K in (0, 7, T_STEPS):   # 0: the whole PML history kept in one forward run; else PML replay
         g = problem.grads(checkpoint_every=K)
+        assert ("whole PML history" if K == 0 else "PML replay") in problem.sim.layout
         np.testing.assert_allclose(g["grad_scale"], problem.g["grad_scale"], rtol=1e-10, atol=0)
         np.testing.assert_allclose(g["grad_source"], problem.g["grad_source"], rtol=1e-10, atol=1e-30)
+    # the segment-recompute path (used where the replay's forcing record does not fit)
+    monkeypatch.setenv("ARD_ADJOINT_RECOMPUTE", "1")
+    g = problem.grads(checkpoint_every=9)
+    assert "segment recompute" in problem.sim.layout
+    np.testing.assert_allclose(g["grad_scale"], problem.g["grad_scale"], rtol=1e-10, atol=0)
+    np.testing.assert_allclose(g["grad_source"], problem.g["grad_source"], rtol=1e-10, atol=1e-30)
+    monkeypatch.delenv("ARD_ADJOINT_RECOMPUTE")
     # without the damping gradient nothing is checkpointed: the other gradients stay
     g = problem.grads(want_scale=False)
     assert g["grad_scale"] is None
