@@ -270,6 +270,7 @@ def adjoint_measurement(A, cfg, scenes, args, device):
     adj_s = time.perf_counter() - t0
     n_air = sum(s.air_cells for s in scenes)
     out = {"workload": f"{cfg['name']} geometry, {S} steps, checkpoint every {args.checkpoint_every}",
+           "path": sim.layout.split("last adjoint: ")[-1],
            "fwd_s": fwd_s, "fwd_adj_s": adj_s, "ratio": adj_s / fwd_s,
            "value": n_air * S / adj_s / 1e9, "unit": UNIT,
            "loss": float(np.sum(g["loss"])),
@@ -296,6 +297,8 @@ def main():
                     help="adjoint checkpoint interval (0: keep the whole PML history when it fits, else automatic)")
     ap.add_argument("--plain", action="store_true", help="one context per scene, run one after another")
     ap.add_argument("--autotune", action="store_true", help="let ard_create time candidate layouts and keep the fastest")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="only the forward + adjoint measurement (one line with the adjoint object)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
@@ -319,6 +322,15 @@ def main():
     h32 = float(np.float32(cfg["h"]))
     scenes = [A.build_scene(sc["air"], sc["sources"], sc["recorders"], h32, cfg["dt"], cfg["c0"], cfg["pml"])
               for sc in cfg["scenes"]]
+    if args.adjoint_only:
+        adj = adjoint_measurement(A, cfg, scenes, args, local)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": adj["value"], "unit": UNIT, "n_gpus": world,
+                              "steps": 1, "warmup": 0, "ms_per_step": adj["fwd_adj_s"] * 1e3,
+                              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                              "data": "synthetic", "config": {"workload": adj["workload"]}, "adjoint": adj}),
+                  flush=True)
+        return 0
     n_air = sum(s.air_cells for s in scenes)
     n_pml = sum(s.pml_cells for s in scenes)
     n_src = sum(len(sc["sources"]) for sc in cfg["scenes"])
