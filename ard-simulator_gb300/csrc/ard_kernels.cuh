@@ -1,20 +1,24 @@
 // sm_103a kernels of the ARD time step.  Templated on the working type T
 // (float: the product path; double: the FP64 GPU oracle).
 //
-// Per step (t, parity par = t & 1):
-//   xform_gemm_kernel   forward 2D DCT-II of the 18 force face layers of every
-//                       air partition (two batched GEMM passes)
+// Per step (t, parity par = t & 1), in launch order:
+//   pml_kernel          Grote-Sim PML update of every slab (own stream)
+//   face2d_kernel       forward 2D DCT-II of the 18 force face layers of every
+//                       air partition, fused per layer pair in shared memory
+//                       (xform_gemm_kernel: the same as two GEMM passes where
+//                       a layer pair does not fit)
 //   modal_kernel        F = expansion of the face transforms (+ point
 //                       sources); M(t) = a (2 cos M(t-1) - M(t-2) + psi F);
 //                       contraction of M(t) onto the face rows and the
 //                       recorder cells
 //   post_modal_kernel   recorder samples of step t + sums of the contraction
 //                       partials
-//   xform_gemm_kernel   inverse 2D transforms -> pressure face layers
-//   pml_kernel          Grote-Sim PML update of every slab
+//   face2d_kernel       inverse 2D transforms -> pressure face layers
 //   iface_kernel        6th-order interface forcing into the force face
 //                       layers / PML strips (owner masks resolve overlapping
 //                       strips in the reference's list order)
+// The air partitions' kernels (face, modal, sums) launch once per air group
+// (up to two groups on two streams).
 #pragma once
 
 #include <cuda_runtime.h>
