@@ -543,7 +543,8 @@ struct ModalArgs {
 // slots, point coefficients, recorder reduction, and the double-buffered
 // per-plane inputs (7 four-element rows per thread + 6 PX values per ky row).
 constexpr int kModalRySlot = 3 * 1024;  // [3 n][rpc * kxt = 1024]
-constexpr int kModalStage = 7 * 4 * kModalThreads + 32 * 6;
+constexpr int kModalStageCz = 7 * 4 * kModalThreads + 32 * 6;   // [8 warps][4]: Cd row kz, n = 0..2
+constexpr int kModalStage = kModalStageCz + 32;
 constexpr int kModalSmemElems =
     2 * kModalRySlot + 2 * kMaxPointsPerPart * 128 + 8 * kMaxPointsPerPart + 2 * kModalStage;
 
@@ -674,26 +675,38 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
     const T* tabB = buf + D.tabB;
     const T damping = (T)D.damping;
 
-    // this thread's ky-contraction outputs: up to 3 of the 6 KXT (parity, row, kx) columns
-    const int rmax = min(RPC, h - ky0);
-    // (slot offset | first row << 16, or -1; output offset from RY, 32-bit)
-    int yo[3], yg[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      const int o = tid + q * kModalThreads;
-      yo[q] = -1; yg[q] = 0;
-      if (o < 6 * KXT) {
-        const int pm = o / (3 * KXT);
-        const int rem = o - pm * 3 * KXT;
-        const int n = rem / KXT, kl = rem - n * KXT;
-        const int kx = tl.y * KXT + kl;
-        if (kx < wp) {
-          yo[q] = (n * 1024 + kl) | ((((ky0 & 1) == pm) ? 0 : 1) << 16);
-          yg[q] = (int)(((long long)tl.z * 6 + pm * 3 + n) * planeY + kx);
-        }
+    // ky contraction.  A warp holds rpw = 32 / G ky rows; with G = 8 the rows
+    // r and r + 2 (same parity) are folded by one shuffle, so every warp leaves
+    // rfold <= 2 partial rows in the slot, at [(warp rfold + row) 3 + n][kxt].
+    // Rows past h carry zeros (their modes are masked).  The parity of a
+    // partial row is (warp rpw + row) & 1 (ky0 is even).  Reducers: one
+    // thread per (parity pm, n, kx quad) sums the warps' partials of parity pm
+    // (start (pm 3 + n) kxt + 4 kq, stride 6 kxt: 8 terms, or 4 when a warp
+    // holds a single row and only every other warp has parity pm).
+    const int rpw = 32 / G;
+    const int rfold = rpw < 2 ? rpw : 2;
+    const int yrow = lane / G;                       // row within the warp
+    const bool ywrite = yrow < rfold;
+    const int yslot = (warp * rfold + (ywrite ? yrow : 0)) * 3 * KXT + kl0;
+    const int nquad = KXT / 4;
+    const int yterms = rfold == 2 ? 8 : 4;
+    int ysrc = -1;
+    T* ydst = buf;
+    if (tid < 6 * nquad) {
+      const int pm = tid / (3 * nquad);
+      const int rem = tid - pm * 3 * nquad;
+      const int n = rem / nquad, kq = rem - n * nquad;
+      const int kx = tl.y * KXT + 4 * kq;
+      if (kx < wp) {
+        ysrc = (pm * 3 + n) * KXT + 4 * kq;
+        ydst = buf + D.RY + ((long long)tl.z * 6 + pm * 3 + n) * planeY + kx;
       }
     }
-    T* const RYb = buf + D.RY;
+    // kx contraction output of this lane (after the reduce-scatter below):
+    // q = parity 3 + n for lanes whose low bits below G / 8 are zero
+    const int xq = li / (G >> 3);
+    const bool xwrite = rowok && (li & ((G >> 3) - 1)) == 0 && xq < 6;
+    T* const xdst = buf + D.RX + ((long long)tl.y * 6 + (xwrite ? xq : 0)) * planeX + (rowok ? ky : 0);
 
     // per-plane inputs of plane kz into stage buffer sb (asynchronous)
     auto issue = [&](int kz, int sb) {
@@ -712,6 +725,7 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
         cp_async_scalar(st + 7 * 4 * kModalThreads + rs * 6 + li,
                         PX + (pm * 3 + n) * planeX + (long long)kz * h + (rowok ? ky : 0), rowok);
       }
+      if (lane < 3) cp_async_scalar(st + kModalStageCz + warp * 4 + lane, Cd + (long long)kz * d + lane, true);
     };
 
     auto body = [&](auto parity, int kz, int sb) {
@@ -719,7 +733,7 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
       const T* st = stage + sb * kModalStage;
       T cz[3];
 #pragma unroll
-      for (int n = 0; n < 3; ++n) cz[n] = Cd[(long long)kz * d + n];
+      for (int n = 0; n < 3; ++n) cz[n] = st[kModalStageCz + warp * 4 + n];
       const T wz = (kz == 0) ? (T)0.5 : (T)1;
       const T wzc = ADJ ? (T)1 : wz;
       T px[2][3];
@@ -800,34 +814,53 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
         }
         if (lanok) store4(Mout + row, Mn);
       }
-      // contraction along kz (registers) and ky (shared memory, reduced below)
+      // contraction along kz (registers) and ky (folded partial rows in the slot)
       T* slot = ry_s + PZ * kModalRySlot;
+      {
+        T ry[3][4];
 #pragma unroll
-      for (int n = 0; n < 3; ++n) {
-        T ry[4];
+        for (int n = 0; n < 3; ++n)
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          rz[PZ][n][e] += wzc * cz[n] * Mn[e];
-          ry[e] = wyc * cy[n] * Mn[e];
+          for (int e = 0; e < 4; ++e) {
+            rz[PZ][n][e] += wzc * cz[n] * Mn[e];
+            ry[n][e] = wyc * cy[n] * Mn[e];
+          }
+        if (rfold == 2 && rpw == 4) {
+#pragma unroll
+          for (int n = 0; n < 3; ++n)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) ry[n][e] += __shfl_xor_sync(0xffffffffu, ry[n][e], 16);
         }
-        store4(slot + n * 1024 + rs * KXT + kl0, ry);
+        if (ywrite) {
+#pragma unroll
+          for (int n = 0; n < 3; ++n) store4(slot + yslot + n * KXT, ry[n]);
+        }
       }
-      // contraction along kx: even / odd kx sums, butterfly over the row's lanes
-      T v[6];
+      // contraction along kx: even / odd kx sums v[q], q = parity 3 + n (two
+      // zero pads), then a reduce-scatter over the row's G lanes: three
+      // halving exchanges leave lane li with q = li / (G / 8), completed by a
+      // butterfly over the G / 8 lanes that share it
+      {
+        T v[8];
 #pragma unroll
-      for (int n = 0; n < 3; ++n) {
-        v[n] = wxc * cx[0][n] * Mn[0] + cx[2][n] * Mn[2];
-        v[3 + n] = cx[1][n] * Mn[1] + cx[3][n] * Mn[3];
-      }
-      for (int o = G >> 1; o > 0; o >>= 1)
+        for (int n = 0; n < 3; ++n) {
+          v[n] = wxc * cx[0][n] * Mn[0] + cx[2][n] * Mn[2];
+          v[3 + n] = cx[1][n] * Mn[1] + cx[3][n] * Mn[3];
+        }
+        v[6] = 0;
+        v[7] = 0;
+        const int o4 = G >> 1, o2 = G >> 2, o1 = G >> 3;
+        const bool u4 = (li & o4) != 0, u2 = (li & o2) != 0, u1 = (li & o1) != 0;
+        T h4[4], h2[2];
 #pragma unroll
-        for (int q = 0; q < 6; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
-      if (rowok && li < 6) {
-        T val = v[0];
+        for (int i = 0; i < 4; ++i)
+          h4[i] = (u4 ? v[4 + i] : v[i]) + __shfl_xor_sync(0xffffffffu, u4 ? v[i] : v[4 + i], o4);
 #pragma unroll
-        for (int q = 1; q < 6; ++q)
-          if (li == q) val = v[q];
-        buf[D.RX + ((long long)tl.y * 6 + li) * planeX + (long long)kz * h + ky] = val;
+        for (int i = 0; i < 2; ++i)
+          h2[i] = (u2 ? h4[2 + i] : h4[i]) + __shfl_xor_sync(0xffffffffu, u2 ? h4[i] : h4[2 + i], o2);
+        T h1 = (u1 ? h2[1] : h2[0]) + __shfl_xor_sync(0xffffffffu, u1 ? h2[0] : h2[1], o1);
+        for (int o = o1 >> 1; o > 0; o >>= 1) h1 += __shfl_xor_sync(0xffffffffu, h1, o);
+        if (xwrite) xdst[(long long)kz * h] = h1;
       }
       for (int r = 0; r < nout; ++r) {
         const T coef = Oh[(long long)kyc * h + pts_y[1][r]] * Od[(long long)kz * d + pts_z[1][r]];
@@ -836,14 +869,16 @@ __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a)
         racc[r] += coef * (c[0] * Mn[0] + c[1] * Mn[1] + c[2] * Mn[2] + c[3] * Mn[3]);
       }
       __syncthreads();
-      // ky contraction of this kz: sum the tile's rows of matching parity
+      // ky contraction of this kz: sums of the warps' partial rows of parity pm
+      if (ysrc >= 0) {
+        T sum[4] = {0, 0, 0, 0};
+        for (int k = 0; k < yterms; ++k) {
+          T p4[4];
+          load4(slot + ysrc + k * 6 * KXT, p4);
 #pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        if (yo[q] < 0) continue;
-        const int so = yo[q] & 0xffff;
-        T sum = 0;
-        for (int r = yo[q] >> 16; r < rmax; r += 2) sum += slot[so + r * KXT];
-        RYb[yg[q] + kz * wp] = sum;
+          for (int e = 0; e < 4; ++e) sum[e] += p4[e];
+        }
+        store4(ydst + (long long)kz * wp, sum);
       }
     };
 
