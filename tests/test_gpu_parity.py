@@ -226,12 +226,12 @@ def test_autotuned_context_matches_default():
 
 
 def test_gemm_face_transforms_fp64_match_oracle():
-    """A 100 x 100 face in FP64 does not fit the fused face kernel's shared
-    memory: the two-pass GEMM transforms run; FP64 GPU against the FP64 C
-    oracle to 1e-10."""
+    """A face of 140 rows is beyond the fused face kernel (128 rows): the
+    two-pass GEMM transforms run; FP64 GPU against the FP64 C oracle to
+    1e-10."""
     dh, c0 = 0.1, 343.0
     dt = float(np.float32(0.5 * dh / (c0 * np.sqrt(3.0))))
-    air, srcs, recs = [(0, 0, 0, 100, 100, 16)], [(30, 40, 8)], [(60, 55, 8), (20, 80, 7)]
+    air, srcs, recs = [(0, 0, 0, 140, 140, 16)], [(30, 40, 8)], [(60, 55, 8), (20, 80, 7)]
     T = 30
     series = (np.hanning(T) * 1e3).astype(np.float32)
     flat = O.make_flat_scene(air, srcs, recs, dict(dh=dh, dt=dt, c0=c0, pml_layers=5))
@@ -246,6 +246,30 @@ def test_gemm_face_transforms_fp64_match_oracle():
     got = sim.recorders(f64=True)
     for r in range(want.shape[1]):
         assert rel_l2(got[:, r], want[:, r]) < F64_TOL, r
+
+
+def test_fused_face_kernel_fp64_large_and_ragged_faces():
+    """The fused face kernel in FP64 near its shared-memory limit: 80-row
+    faces (two rows per thread, split 16-column jobs) and ragged extents (rows
+    not a multiple of 4: scalar staging); against the FP64 C oracle to 1e-10."""
+    dh, c0 = 0.1, 343.0
+    dt = float(np.float32(0.5 * dh / (c0 * np.sqrt(3.0))))
+    for air, srcs, recs in (([(0, 0, 0, 80, 80, 16)], [(30, 40, 8)], [(60, 55, 8), (20, 70, 7)]),
+                            ([(0, 0, 0, 97, 61, 13)], [(40, 30, 6)], [(50, 33, 6), (20, 40, 7)])):
+        T = 30
+        series = (np.hanning(T) * 1e3).astype(np.float32)
+        flat = O.make_flat_scene(air, srcs, recs, dict(dh=dh, dt=dt, c0=c0, pml_layers=5))
+        ref = O.OracleSim(flat, "f64")
+        ref.set_source_series(0, series)
+        ref.step(T)
+        want = ref.recorders()
+        sim = A.Simulation(A.build_scene(air, srcs, recs, dh, dt, c0, 5), precision=A.PREC_F64, max_steps=T)
+        assert "fused" in sim.layout
+        sim.set_source_series(0, series)
+        sim.run(T)
+        got = sim.recorders(f64=True)
+        for r in range(want.shape[1]):
+            assert rel_l2(got[:, r], want[:, r]) < F64_TOL, (air, r)
 
 
 def test_write_outputs_in_reference_format(tmp_path):
@@ -296,7 +320,7 @@ def test_edge_cases_empty_and_ragged():
 
 
 def test_gemm_face_transforms_fp32_match_oracle():
-    """200 x 200 faces in FP32 exceed the fused kernel's shared memory: the
+    """200 x 200 faces in FP32 exceed the fused kernel's 128 rows: the
     two-pass GEMM face transforms run; FP32 against the FP64 C oracle within
     the FP32 bar (recorders a few cells from the source, reached in time)."""
     dh, c0 = 0.1, 343.0
