@@ -12,6 +12,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "ard_device.cuh"
@@ -302,6 +303,26 @@ extern "C" int ard_synchronize(ard_ctx* c) {
 
 namespace ard {
 
+// Launch of a step kernel with programmatic stream serialization: the grid is
+// scheduled while its predecessor in the stream drains and waits for it on
+// the device (grid_dependency_wait), which hides the launch gap between the
+// dependent kernels of a step (also inside the captured graphs).
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_dep(void (*kernel)(KArgs...), long long grid, int block, size_t smem, cudaStream_t s,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 // Stage order of one step; with `ev` (kNumStages + 1 events, direct launches
 // on one stream) event k is recorded before stage k and event kNumStages
 // after the last stage.
@@ -339,16 +360,16 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
         if (ctx->fused_faces) {
           const int n = G.f_hi - G.f_lo;
           if (n > 0)
-            face2d_kernel<T><<<grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st>>>(buf, ctx->d_fwd2d + G.f_lo, n,
-                                                                                         ctx->f2d_smem);
+            ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st, buf,
+                                ctx->d_fwd2d + G.f_lo, n, ctx->f2d_smem));
         } else {
-          xform_gemm_kernel<T><<<grid_for(ctx->fwd1.units, 1, gx), 256, 0, st>>>(
-              buf, ctx->d_fwd1, (int)ctx->fwd1.jobs.size(), ctx->fwd1.units);
+          ARD_CUDA(launch_dep(xform_gemm_kernel<T>, grid_for(ctx->fwd1.units, 1, gx), 256, 0, st, buf, ctx->d_fwd1,
+                              (int)ctx->fwd1.jobs.size(), ctx->fwd1.units));
         }
       } else if (k == kStageFwdCols) {
         if (!ctx->fused_faces)
-          xform_gemm_kernel<T><<<grid_for(ctx->fwd2.units, 1, gx), 256, 0, st>>>(
-              buf, ctx->d_fwd2, (int)ctx->fwd2.jobs.size(), ctx->fwd2.units);
+          ARD_CUDA(launch_dep(xform_gemm_kernel<T>, grid_for(ctx->fwd2.units, 1, gx), 256, 0, st, buf, ctx->d_fwd2,
+                              (int)ctx->fwd2.jobs.size(), ctx->fwd2.units));
       } else if (k == kStageModal) {
         const int n = G.t_hi - G.t_lo;
         if (n > 0) {
@@ -356,9 +377,9 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
                           ctx->d_series, ctx->max_steps, ctx->d_t, tstep, par};
           const int mgrid = grid_for(n, 1, ctx->num_sms * 2);
           if (ctx->arith == ARD_ARITH_REFERENCE)
-            modal_kernel<T, true><<<mgrid, kModalThreads, msmem, st>>>(ma);
+            ARD_CUDA(launch_dep(modal_kernel<T, true, false>, mgrid, kModalThreads, msmem, st, ma));
           else
-            modal_kernel<T, false><<<mgrid, kModalThreads, msmem, st>>>(ma);
+            ARD_CUDA(launch_dep(modal_kernel<T, false, false>, mgrid, kModalThreads, msmem, st, ma));
         }
       } else if (k == kStageRecorder) {
         return launch_post_modal_range<T>(ctx, st, tstep, G.r_lo, G.r_hi, G.s_lo, G.s_hi, G.s_first, G.s_total);
@@ -366,16 +387,16 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
         if (ctx->fused_faces) {
           const int n = G.i_hi - G.i_lo;
           if (n > 0)
-            face2d_kernel<T><<<grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st>>>(buf, ctx->d_inv2d + G.i_lo, n,
-                                                                                         ctx->f2d_smem);
+            ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st, buf,
+                                ctx->d_inv2d + G.i_lo, n, ctx->f2d_smem));
         } else {
-          xform_gemm_kernel<T><<<grid_for(ctx->inv1.units, 1, gx), 256, 0, st>>>(
-              buf, ctx->d_inv1, (int)ctx->inv1.jobs.size(), ctx->inv1.units);
+          ARD_CUDA(launch_dep(xform_gemm_kernel<T>, grid_for(ctx->inv1.units, 1, gx), 256, 0, st, buf, ctx->d_inv1,
+                              (int)ctx->inv1.jobs.size(), ctx->inv1.units));
         }
       } else if (k == kStageInvRows) {
         if (!ctx->fused_faces)
-          xform_gemm_kernel<T><<<grid_for(ctx->inv2.units, 1, gx), 256, 0, st>>>(
-              buf, ctx->d_inv2, (int)ctx->inv2.jobs.size(), ctx->inv2.units);
+          ARD_CUDA(launch_dep(xform_gemm_kernel<T>, grid_for(ctx->inv2.units, 1, gx), 256, 0, st, buf, ctx->d_inv2,
+                              (int)ctx->inv2.jobs.size(), ctx->inv2.units));
       }
       ARD_CUDA(cudaGetLastError());
       return ARD_OK;
@@ -406,7 +427,7 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
   if (ctx->n_face_cells > 0) {
     IfaceArgs<T> ia{buf, ctx->d_ifs, ctx->d_cell_iface, ctx->n_face_cells, ctx->d_mask, par, (T)ctx->c0,
                     (T)ctx->dh};
-    iface_kernel<T><<<grid_for(ctx->n_face_cells, 256, ctx->num_sms * 16), 256, 0, s>>>(ia);
+    ARD_CUDA(launch_dep(iface_kernel<T>, grid_for(ctx->n_face_cells, 256, ctx->num_sms * 16), 256, 0, s, ia));
     ARD_CUDA(cudaGetLastError());
   }
   ARD_CUDA(mark(kNumStages));
@@ -419,7 +440,7 @@ int launch_pml(Ctx* ctx, int par, int tstep, cudaStream_t s) {
   if (ctx->pml_blocks.empty()) return ARD_OK;
   PmlArgs<T> pa{reinterpret_cast<T*>(ctx->d_buf), ctx->d_pml, ctx->d_pml_blocks, (int)ctx->pml_blocks.size(), par,
                 (T)ctx->dt, (T)ctx->dh, (T)ctx->c0, (const PmlHist<T>*)ctx->d_phist, ctx->d_t, tstep};
-  pml_kernel<T><<<grid_for((long long)ctx->pml_blocks.size(), 1, ctx->num_sms * 8), 256, 0, s>>>(pa);
+  ARD_CUDA(launch_dep(pml_kernel<T>, grid_for((long long)ctx->pml_blocks.size(), 1, ctx->num_sms * 8), 256, 0, s, pa));
   ARD_CUDA(cudaGetLastError());
   return ARD_OK;
 }
@@ -439,7 +460,7 @@ int launch_post_modal_range(Ctx* ctx, cudaStream_t s, int tstep, int r_lo, int r
   PostModalArgs<T> a{reinterpret_cast<T*>(ctx->d_buf), ctx->d_dct, ctx->d_recpts, r_lo, nrec, ctx->n_rec_total,
                      ctx->d_hist, ctx->d_t, tstep, ctx->max_steps, rec_blocks, ctx->d_psum + s_lo, s_hi - s_lo,
                      s_first, s_total};
-  post_modal_kernel<T><<<rec_blocks + sum_blocks, 256, 0, s>>>(a);
+  ARD_CUDA(launch_dep(post_modal_kernel<T>, rec_blocks + sum_blocks, 256, 0, s, a));
   ARD_CUDA(cudaGetLastError());
   return ARD_OK;
 }

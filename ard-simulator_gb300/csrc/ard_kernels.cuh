@@ -89,6 +89,13 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// Programmatic dependent launch: a step kernel launched with programmatic
+// stream serialization may start while its predecessor in the stream is
+// finishing; griddepcontrol.wait returns once the predecessor has completed
+// and its writes are visible (at once for an ordinary launch).  Every step
+// kernel waits before its first global access.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -120,6 +127,7 @@ __device__ __forceinline__ T job_input(const T* __restrict__ buf, const XformJob
 template <typename T>
 __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, const XformJob* __restrict__ jobs,
                                                           int njobs, int total) {
+  grid_dependency_wait();
   // two K-chunk buffers: chunk k+1 is fetched into registers while chunk k is
   // multiplied; chunks of 16 k (32 measured slower)
   constexpr int BK = 16;
@@ -284,6 +292,7 @@ struct PostModalArgs {
 
 template <typename T>
 __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
+  grid_dependency_wait();
   if ((int)blockIdx.x < a.rec_blocks) {
     const int lane = threadIdx.x & 31;
     const int rl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -352,6 +361,7 @@ __host__ __device__ inline int face2d_pitch(int n) {
 template <typename T>
 __global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ buf, const Face2DJob* __restrict__ jobs,
                                                       int njobs, Face2DSmem sm) {
+  grid_dependency_wait();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* X0 = reinterpret_cast<T*>(smem_raw);
   T* X1 = X0 + sm.xs;
@@ -566,6 +576,7 @@ constexpr int kModalSmemElems =
 // source cells (source-series gradient partials).
 template <typename T, bool REF, bool ADJ = false>
 __global__ void __launch_bounds__(kModalThreads, 2) modal_kernel(ModalArgs<T> a) {
+  grid_dependency_wait();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* ry_s = reinterpret_cast<T*>(smem_raw);
   T* cws = ry_s + 2 * kModalRySlot;                  // [kMaxPointsPerPart][128]
@@ -975,6 +986,7 @@ struct PmlArgs {
 // memory per layer; the normal-axis stencils run from a register window.
 template <typename T>
 __global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
+  grid_dependency_wait();
   constexpr int TA = 8, TB = 32;
   __shared__ T Ps[TA + 6][TB + 6];
   __shared__ T FA[TA + 4][TB];
@@ -1174,6 +1186,7 @@ __device__ __forceinline__ long long side_force_offset(const SideDev& S, int typ
 // reference's list-order overwrites.
 template <typename T>
 __global__ void __launch_bounds__(256) iface_kernel(IfaceArgs<T> a) {
+  grid_dependency_wait();
   const T C[6][6] = {{0, 0, -2, 2, 0, 0},       {0, -2, 27, -27, 2, 0},     {-2, 27, -270, 270, -27, 2},
                      {2, -27, 270, -270, 27, -2}, {0, 2, -27, 27, -2, 0},     {0, 0, 2, -2, 0, 0}};
   const T k0 = a.c0 * a.c0 / ((T)180 * a.dh * a.dh);
