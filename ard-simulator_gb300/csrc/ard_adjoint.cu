@@ -69,6 +69,7 @@ int configure_adjoint(Ctx* ctx) {
   if (ctx->fused_faces)
     ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   std::max(ctx->smem_optin, (int)ctx->f2d_bytes)));
+  ARD_CUDA(configure_face_gemm<T>());
   return ARD_OK;
 }
 
@@ -115,8 +116,8 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
           buf, ctx->d_adj1_2d, (int)ctx->adj1_2d.size(), ctx->f2d_smem);
     } else {
       for (int k = 0; k < 2; ++k)
-        xform_gemm_kernel<T><<<grid_for(ctx->adjg[k].units, 1, gx), 256, 0, s>>>(
-            buf, ctx->d_adjg[k], (int)ctx->adjg[k].jobs.size(), ctx->adjg[k].units);
+        ARD_CUDA(launch_face_gemm<T>(buf, ctx->adjg[k].jobs[0], ctx->d_adjg[k], (int)ctx->adjg[k].jobs.size(),
+                                     ctx->adjg[k].units, grid_for(ctx->adjg[k].units, 1, ctx->num_sms * 2), s));
     }
     ARD_CUDA(cudaGetLastError());
     ModalArgs<T> ma{buf, ctx->d_dct, ctx->d_tiles, (int)ctx->tiles.size(), ctx->d_srcpts, ctx->d_recpts,
@@ -139,8 +140,8 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
           buf, ctx->d_adj2_2d, (int)ctx->adj2_2d.size(), ctx->f2d_smem);
     } else {
       for (int k = 2; k < 4; ++k)
-        xform_gemm_kernel<T><<<grid_for(ctx->adjg[k].units, 1, gx), 256, 0, s>>>(
-            buf, ctx->d_adjg[k], (int)ctx->adjg[k].jobs.size(), ctx->adjg[k].units);
+        ARD_CUDA(launch_face_gemm<T>(buf, ctx->adjg[k].jobs[0], ctx->d_adjg[k], (int)ctx->adjg[k].jobs.size(),
+                                     ctx->adjg[k].units, grid_for(ctx->adjg[k].units, 1, ctx->num_sms * 2), s));
     }
     ARD_CUDA(cudaGetLastError());
   }

@@ -106,6 +106,7 @@ static int configure_kernels(Ctx* ctx) {
     if (ctx->fused_faces)
       ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, f2d));
   }
+  ARD_CUDA(ctx->prec == ARD_PREC_F64 ? configure_face_gemm<double>() : configure_face_gemm<float>());
   return ARD_OK;
 }
 
@@ -303,26 +304,6 @@ extern "C" int ard_synchronize(ard_ctx* c) {
 
 namespace ard {
 
-// Launch of a step kernel with programmatic stream serialization: the grid is
-// scheduled while its predecessor in the stream drains and waits for it on
-// the device (grid_dependency_wait), which hides the launch gap between the
-// dependent kernels of a step (also inside the captured graphs).
-template <typename... KArgs, typename... Args>
-static cudaError_t launch_dep(void (*kernel)(KArgs...), long long grid, int block, size_t smem, cudaStream_t s,
-                              Args&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3((unsigned)block);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
-}
-
 // Stage order of one step; with `ev` (kNumStages + 1 events, direct launches
 // on one stream) event k is recorded before stage k and event kNumStages
 // after the last stage.
@@ -363,13 +344,13 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
             ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st, buf,
                                 ctx->d_fwd2d + G.f_lo, n, ctx->f2d_smem));
         } else {
-          ARD_CUDA(launch_dep(xform_gemm_kernel<T>, grid_for(ctx->fwd1.units, 1, gx), 256, 0, st, buf, ctx->d_fwd1,
-                              (int)ctx->fwd1.jobs.size(), ctx->fwd1.units));
+          ARD_CUDA(launch_face_gemm<T>(buf, ctx->fwd1.jobs[0], ctx->d_fwd1, (int)ctx->fwd1.jobs.size(), ctx->fwd1.units,
+                                        grid_for(ctx->fwd1.units, 1, ctx->num_sms * 2), st));
         }
       } else if (k == kStageFwdCols) {
         if (!ctx->fused_faces)
-          ARD_CUDA(launch_dep(xform_gemm_kernel<T>, grid_for(ctx->fwd2.units, 1, gx), 256, 0, st, buf, ctx->d_fwd2,
-                              (int)ctx->fwd2.jobs.size(), ctx->fwd2.units));
+          ARD_CUDA(launch_face_gemm<T>(buf, ctx->fwd2.jobs[0], ctx->d_fwd2, (int)ctx->fwd2.jobs.size(), ctx->fwd2.units,
+                                        grid_for(ctx->fwd2.units, 1, ctx->num_sms * 2), st));
       } else if (k == kStageModal) {
         const int n = G.t_hi - G.t_lo;
         if (n > 0) {
@@ -390,13 +371,13 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
             ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st, buf,
                                 ctx->d_inv2d + G.i_lo, n, ctx->f2d_smem));
         } else {
-          ARD_CUDA(launch_dep(xform_gemm_kernel<T>, grid_for(ctx->inv1.units, 1, gx), 256, 0, st, buf, ctx->d_inv1,
-                              (int)ctx->inv1.jobs.size(), ctx->inv1.units));
+          ARD_CUDA(launch_face_gemm<T>(buf, ctx->inv1.jobs[0], ctx->d_inv1, (int)ctx->inv1.jobs.size(), ctx->inv1.units,
+                                        grid_for(ctx->inv1.units, 1, ctx->num_sms * 2), st));
         }
       } else if (k == kStageInvRows) {
         if (!ctx->fused_faces)
-          ARD_CUDA(launch_dep(xform_gemm_kernel<T>, grid_for(ctx->inv2.units, 1, gx), 256, 0, st, buf, ctx->d_inv2,
-                              (int)ctx->inv2.jobs.size(), ctx->inv2.units));
+          ARD_CUDA(launch_face_gemm<T>(buf, ctx->inv2.jobs[0], ctx->d_inv2, (int)ctx->inv2.jobs.size(), ctx->inv2.units,
+                                        grid_for(ctx->inv2.units, 1, ctx->num_sms * 2), st));
       }
       ARD_CUDA(cudaGetLastError());
       return ARD_OK;

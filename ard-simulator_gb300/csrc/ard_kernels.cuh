@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <type_traits>
+#include <utility>
 
 #include "ard_device.cuh"
 
@@ -250,6 +251,260 @@ __global__ void __launch_bounds__(256) xform_gemm_kernel(T* __restrict__ buf, co
       }
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Face transforms of the step as GEMM passes (faces too large for the fused
+// kernel): the same jobs as xform_gemm_kernel, with both operands staged by
+// cp.async into a three-deep ring of 32-wide K chunks (no register staging,
+// one barrier per chunk).  An operand whose source is contiguous along K
+// ("k-contiguous": the X lines of a row pass, the forward tables) is kept
+// [m or n][32 k] with its 16-byte chunks XOR-swizzled by (row / 4) % 8; an
+// operand contiguous along m or n is kept [32 k][64 + 4].  The pass's input
+// combination X = in0 + sgn in1 is formed when the X operand is read.
+// Instances (one per job list, all jobs of a list alike):
+//   PK, QK = 1, 1, CP: row pass, forward  (P = X lines, Q(k, n) = A[n K + k])
+//   PK, QK = 1, 0:     column pass, forward (P = A[m K + k], Q = X rows) and
+//                      row pass, inverse (P = X lines, Q(k, n) = A[k K + n])
+//   PK, QK = 0, 0, CQ: column pass, inverse (P(m, k) = A[k K + m], Q = X rows)
+// ---------------------------------------------------------------------------
+
+constexpr int kGemmBK = 32;
+constexpr int kGemmStages = 3;
+constexpr int kGemmTile = kGemmBK * 68;   // elements of one staged operand tile (either layout)
+__host__ __device__ constexpr int face_gemm_smem_elems(bool comb) { return kGemmStages * (comb ? 3 : 2) * kGemmTile; }
+
+// k-contiguous tile: element (r, k) of the [64][32] tile
+__device__ __forceinline__ int kc_index(int r, int k) { return r * kGemmBK + ((((k >> 2) ^ (r >> 2)) & 7) << 2) + (k & 3); }
+
+template <typename T, bool PK, bool QK, bool CP, bool CQ>
+__global__ void __launch_bounds__(256, 2) face_gemm_kernel(T* __restrict__ buf, const XformJob* __restrict__ jobs,
+                                                            int njobs, int total) {
+  grid_dependency_wait();
+  constexpr bool COMB = CP || CQ;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  constexpr int kMaxCachedJobs = 1024;
+  __shared__ int sfirst[kMaxCachedJobs];
+  const int tid = threadIdx.x;
+  const int ty = tid >> 4, tx = tid & 15;
+  const bool cached = njobs <= kMaxCachedJobs;
+  if (cached)
+    for (int i = tid; i < njobs; i += 256) sfirst[i] = jobs[i].first;
+  __syncthreads();
+  for (int unit = blockIdx.x; unit < total; unit += gridDim.x) {
+    int ji;
+    if (cached) {
+      int lo = 0, hi = njobs - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sfirst[mid] <= unit) lo = mid; else hi = mid - 1;
+      }
+      ji = lo;
+    } else {
+      ji = find_job(jobs, njobs, unit);
+    }
+    const XformJob J = jobs[ji];
+    const int t = unit - J.first;
+    const int m0 = (t / J.tn) * 64, n0 = (t % J.tn) * 64;
+    const int Md = J.rows ? J.batch : J.n;
+    const int Nd = J.rows ? J.n : J.batch;
+    const int K = J.n;
+    // operand sources: P (m, k) and Q (k, n); the X operand may have a second input
+    long long p0, p1 = 0, q0, q1 = 0;
+    int sp, sq;
+    if (J.rows) { p0 = J.in0; p1 = J.in1; sp = J.ld; q0 = J.ctab; sq = K; }
+    else { p0 = J.ctab; sp = K; q0 = J.in0; q1 = J.in1; sq = J.ld; }
+    const T sgn = (T)J.sgn;
+    // stage one operand tile: rows of the k-contiguous layout are m (or n),
+    // rows of the other layout are k; lim = extent of m (or n)
+    auto stage_kc = [&](T* dst, long long base, int stride, int r0, int lim, int k0) {
+      const bool vec = ((stride | K) & 3) == 0 && (base & 3) == 0;
+      if (vec) {
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          const int e = tid + 256 * v;          // 512 vectors: row e / 8, chunk e % 8
+          const int r = e >> 3, c = e & 7;
+          const bool ok = r0 + r < lim && k0 + 4 * c < K;
+          cp_async4(dst + kc_index(r, 4 * c), buf + (ok ? base + (long long)(r0 + r) * stride + k0 + 4 * c : 0), ok);
+        }
+      } else {
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+          const int e = tid + 256 * v;          // 2048 elements: row e / 32, k e % 32
+          const int r = e >> 5, k = e & 31;
+          const bool ok = r0 + r < lim && k0 + k < K;
+          cp_async_scalar(dst + kc_index(r, k), buf + (ok ? base + (long long)(r0 + r) * stride + k0 + k : 0), ok);
+        }
+      }
+    };
+    auto stage_mn = [&](T* dst, long long base, int stride, int c0, int lim, int k0) {
+      const bool vec = ((stride | lim) & 3) == 0 && (base & 3) == 0;
+      if (vec) {
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          const int e = tid + 256 * v;          // 512 vectors: k e / 16, columns 4 (e % 16)
+          const int k = e >> 4, c = (e & 15) * 4;
+          const bool ok = k0 + k < K && c0 + c < lim;
+          cp_async4(dst + k * 68 + c, buf + (ok ? base + (long long)(k0 + k) * stride + c0 + c : 0), ok);
+        }
+      } else {
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+          const int e = tid + 256 * v;          // 2048 elements: k e / 64, column e % 64
+          const int k = e >> 6, c = e & 63;
+          const bool ok = k0 + k < K && c0 + c < lim;
+          cp_async_scalar(dst + k * 68 + c, buf + (ok ? base + (long long)(k0 + k) * stride + c0 + c : 0), ok);
+        }
+      }
+    };
+    constexpr int NT = COMB ? 3 : 2;
+    auto issue = [&](int k0, int sb) {
+      T* st = sm + sb * NT * kGemmTile;
+      if constexpr (PK) stage_kc(st, p0, sp, m0, Md, k0); else stage_mn(st, p0, sp, m0, Md, k0);
+      if constexpr (QK) stage_kc(st + kGemmTile, q0, sq, n0, Nd, k0); else stage_mn(st + kGemmTile, q0, sq, n0, Nd, k0);
+      if constexpr (CP) stage_kc(st + 2 * kGemmTile, p1, sp, m0, Md, k0);
+      if constexpr (CQ) stage_mn(st + 2 * kGemmTile, q1, sq, n0, Nd, k0);
+    };
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = 0;
+    const int nch = (K + kGemmBK - 1) / kGemmBK;
+    __syncthreads();   // the previous unit is done with the ring
+#pragma unroll
+    for (int p = 0; p < kGemmStages - 1; ++p) {
+      if (p < nch) issue(p * kGemmBK, p);
+      cp_async_commit();
+    }
+    for (int c = 0; c < nch; ++c) {
+      cp_async_wait<kGemmStages - 2>();
+      __syncthreads();   // chunk c visible; chunk c - 1's slot free
+      if (c + kGemmStages - 1 < nch) issue((c + kGemmStages - 1) * kGemmBK, (c + kGemmStages - 1) % kGemmStages);
+      cp_async_commit();
+      const T* st = sm + (c % kGemmStages) * NT * kGemmTile;
+      const T* Pt = st;
+      const T* Qt = st + kGemmTile;
+      const T* Xt = st + 2 * kGemmTile;
+#pragma unroll 2
+      for (int kq = 0; kq < kGemmBK; kq += 4) {
+        T pa[4][4], qb[4][4];   // [row i or column j][k of the quad]
+        if constexpr (PK) {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            load4(Pt + kc_index(ty * 4 + i, kq), pa[i]);
+            if constexpr (CP) {
+              T x[4];
+              load4(Xt + kc_index(ty * 4 + i, kq), x);
+#pragma unroll
+              for (int k = 0; k < 4; ++k) pa[i][k] += sgn * x[k];
+            }
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            T v[4];
+            load4(Pt + (kq + k) * 68 + ty * 4, v);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) pa[i][k] = v[i];
+          }
+        }
+        if constexpr (QK) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) load4(Qt + kc_index(tx * 4 + j, kq), qb[j]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            T v[4];
+            load4(Qt + (kq + k) * 68 + tx * 4, v);
+            if constexpr (CQ) {
+              T x[4];
+              load4(Xt + (kq + k) * 68 + tx * 4, x);
+#pragma unroll
+              for (int j = 0; j < 4; ++j) v[j] += sgn * x[j];
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) qb[j][k] = v[j];
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] += pa[i][k] * qb[j][k];
+      }
+    }
+    cp_async_wait<0>();
+    const T scale = (T)J.scale;
+    const int nb = n0 + tx * 4;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int m = m0 + ty * 4 + i;
+      if (m >= Md) continue;
+      const long long o = J.out + (long long)m * J.ld + nb;
+      if (nb + 3 < Nd && (o & 3) == 0) {
+        T v[4] = {acc[i][0] * scale, acc[i][1] * scale, acc[i][2] * scale, acc[i][3] * scale};
+        store4(buf + o, v);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (nb + j < Nd) buf[o + j] = acc[i][j] * scale;
+      }
+    }
+  }
+}
+
+// Host: a step kernel launched with programmatic stream serialization: the
+// grid is scheduled while its predecessor in the stream drains and waits for
+// it on the device (grid_dependency_wait), which hides the launch gap between
+// the dependent kernels of a step (also inside the captured graphs).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dep(void (*kernel)(KArgs...), long long grid, int block, size_t smem, cudaStream_t s,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+// Host: the face_gemm_kernel instance for a job list (all jobs of a list share
+// rows, inverse and whether the X operand has a second input), `grid` blocks.
+template <typename T>
+inline cudaError_t launch_face_gemm(T* buf, const XformJob& j0, const XformJob* d_jobs, int njobs, int units, int grid,
+                                    cudaStream_t s) {
+  if (njobs == 0) return cudaSuccess;
+  const bool comb = j0.in1 >= 0;
+  const size_t s2 = (size_t)face_gemm_smem_elems(false) * sizeof(T), s3 = (size_t)face_gemm_smem_elems(true) * sizeof(T);
+  if (j0.rows && !j0.inverse && comb)
+    return launch_dep(face_gemm_kernel<T, true, true, true, false>, grid, 256, s3, s, buf, d_jobs, njobs, units);
+  if (!comb && (j0.rows != 0) == (j0.inverse != 0))
+    return launch_dep(face_gemm_kernel<T, true, false, false, false>, grid, 256, s2, s, buf, d_jobs, njobs, units);
+  if (!j0.rows && j0.inverse && comb)
+    return launch_dep(face_gemm_kernel<T, false, false, false, true>, grid, 256, s3, s, buf, d_jobs, njobs, units);
+  return cudaErrorInvalidValue;
+}
+
+// Host: dynamic shared memory of the face_gemm_kernel instances (set in every
+// translation unit that launches them).
+template <typename T>
+inline cudaError_t configure_face_gemm() {
+  const int s2 = (int)(face_gemm_smem_elems(false) * sizeof(T)), s3 = (int)(face_gemm_smem_elems(true) * sizeof(T));
+  cudaError_t e = cudaFuncSetAttribute(face_gemm_kernel<T, true, true, true, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, s3);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(face_gemm_kernel<T, true, false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s2);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(face_gemm_kernel<T, false, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s3);
+  return e;
 }
 
 // ---------------------------------------------------------------------------
