@@ -93,7 +93,7 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
   if (ctx->n_face_cells > 0) {
     IfaceAdjArgs<T> ia{buf, ctx->d_ifs, (int)ctx->ifs.size(), ctx->n_face_cells, ctx->d_dct, ctx->d_pml,
                        ctx->d_mask, lin, lout, (T)ctx->c0, (T)ctx->dh, (T)ctx->dt};
-    iface_adjoint_kernel<T><<<grid_for(ctx->n_face_cells, 256, ctx->num_sms * 16), 256, 0, s>>>(ia);
+    ARD_CUDA(launch_dep(iface_adjoint_kernel<T>, grid_for(ctx->n_face_cells, 256, ctx->num_sms * 16), 256, 0, s, ia));
     ARD_CUDA(cudaGetLastError());
   }
   const bool fork = !ctx->pml_blocks.empty() && !ctx->dct.empty();
@@ -105,15 +105,15 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
     PmlAdjArgs<T> pa{buf, ctx->d_pml, ctx->d_pml_blocks, (int)ctx->pml_blocks.size(), lin, ly, lout, (t + 1) & 1,
                      (T)ctx->dt, (T)ctx->dh, (T)ctx->c0, (const T*)hv.p, (const T*)hv.phn, hv.hlen, ctx->d_tb,
                      tstep, hv.gz};
-    pml_adjoint_kernel<T><<<grid_for((long long)ctx->pml_blocks.size(), 1, ctx->num_sms * 8), 256, 0,
-                            fork ? s2 : s>>>(pa);
+    ARD_CUDA(launch_dep(pml_adjoint_kernel<T>, grid_for((long long)ctx->pml_blocks.size(), 1, ctx->num_sms * 8), 256,
+                        0, fork ? s2 : s, pa));
     ARD_CUDA(cudaGetLastError());
   }
   if (!ctx->dct.empty()) {
     const int gx = ctx->num_sms * 4;
     if (ctx->fused_faces) {
-      face2d_kernel<T><<<grid_for((long long)ctx->adj1_2d.size(), 1, gx), kFace2DThreads, ctx->f2d_bytes, s>>>(
-          buf, ctx->d_adj1_2d, (int)ctx->adj1_2d.size(), ctx->f2d_smem);
+      ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for((long long)ctx->adj1_2d.size(), 1, gx), kFace2DThreads,
+                          ctx->f2d_bytes, s, buf, ctx->d_adj1_2d, (int)ctx->adj1_2d.size(), ctx->f2d_smem));
     } else {
       for (int k = 0; k < 2; ++k)
         ARD_CUDA(launch_face_gemm<T>(buf, ctx->adjg[k].jobs[0], ctx->d_adjg[k], (int)ctx->adjg[k].jobs.size(),
@@ -125,19 +125,20 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
     const size_t msmem = kModalSmemElems * sizeof(T);
     const int mgrid = grid_for((long long)ctx->tiles.size(), 1, ctx->num_sms * 2);
     if (ctx->arith == ARD_ARITH_REFERENCE)
-      modal_kernel<T, true, true><<<mgrid, kModalThreads, msmem, s>>>(ma);
+      ARD_CUDA(launch_dep(modal_kernel<T, true, true>, mgrid, kModalThreads, msmem, s, ma));
     else
-      modal_kernel<T, false, true><<<mgrid, kModalThreads, msmem, s>>>(ma);
+      ARD_CUDA(launch_dep(modal_kernel<T, false, true>, mgrid, kModalThreads, msmem, s, ma));
     ARD_CUDA(cudaGetLastError());
     if (!ctx->srcpts.empty()) {
-      srcgrad_kernel<T><<<grid_for((long long)ctx->srcpts.size() * 32, 128, 1 << 30), 128, 0, s>>>(
-          buf, ctx->d_dct, ctx->d_srcpts, (int)ctx->srcpts.size(), ctx->n_src_total, ab.gsrc, ctx->d_tb, tstep);
+      ARD_CUDA(launch_dep(srcgrad_kernel<T>, grid_for((long long)ctx->srcpts.size() * 32, 128, 1 << 30), 128, 0, s,
+                          (const T*)buf, ctx->d_dct, ctx->d_srcpts, (int)ctx->srcpts.size(), ctx->n_src_total,
+                          ab.gsrc, ctx->d_tb, tstep));
       ARD_CUDA(cudaGetLastError());
     }
     if (int rc2 = launch_post_modal<T>(ctx, s, 0, false)) return rc2;
     if (ctx->fused_faces) {
-      face2d_kernel<T><<<grid_for((long long)ctx->adj2_2d.size(), 1, gx), kFace2DThreads, ctx->f2d_bytes, s>>>(
-          buf, ctx->d_adj2_2d, (int)ctx->adj2_2d.size(), ctx->f2d_smem);
+      ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for((long long)ctx->adj2_2d.size(), 1, gx), kFace2DThreads,
+                          ctx->f2d_bytes, s, buf, ctx->d_adj2_2d, (int)ctx->adj2_2d.size(), ctx->f2d_smem));
     } else {
       for (int k = 2; k < 4; ++k)
         ARD_CUDA(launch_face_gemm<T>(buf, ctx->adjg[k].jobs[0], ctx->d_adjg[k], (int)ctx->adjg[k].jobs.size(),

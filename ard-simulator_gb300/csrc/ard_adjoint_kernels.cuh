@@ -81,6 +81,7 @@ __device__ __forceinline__ void adj_pressure_add(const IfaceAdjArgs<T>& a, int t
 // the three pressure layers on each side that it was computed from.
 template <typename T>
 __global__ void __launch_bounds__(256) iface_adjoint_kernel(IfaceAdjArgs<T> a) {
+  grid_dependency_wait();
   const T C[6][6] = {{0, 0, -2, 2, 0, 0},       {0, -2, 27, -27, 2, 0},     {-2, 27, -270, 270, -27, 2},
                      {2, -27, 270, -270, 27, -2}, {0, 2, -27, 27, -2, 0},     {0, 0, 2, -2, 0, 0}};
   for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < a.total;
@@ -158,6 +159,7 @@ struct PmlAdjArgs {
 //               - dt Phi_n (phi_n(t) + Dn p(t)) + dt Phi_a Da p(t) + dt Phi_b Db p(t)
 template <typename T>
 __global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
+  grid_dependency_wait();
   constexpr int TA = 8, TB = 32;
   __shared__ T Xs[TA + 6][TB + 6];
   __shared__ T FA[TA + 4][TB];
@@ -355,6 +357,7 @@ template <typename T>
 __global__ void srcgrad_kernel(const T* __restrict__ buf, const DctDev* __restrict__ dct,
                                const PointDev* __restrict__ srcs, int npts, int ld, double* __restrict__ g,
                                const long long* tc, int tstep) {
+  grid_dependency_wait();
   const int lane = threadIdx.x & 31;
   const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (r >= npts) return;
