@@ -5,7 +5,7 @@
 //   pml_kernel          Grote-Sim PML update of every slab (own stream)
 //   face2d_kernel       forward 2D DCT-II of the 18 force face layers of every
 //                       air partition, fused per layer pair in shared memory
-//                       (xform_gemm_kernel: the same as two GEMM passes where
+//                       (face_gemm_kernel: the same as two GEMM passes where
 //                       a layer pair does not fit)
 //   modal_kernel        F = expansion of the face transforms (+ point
 //                       sources); M(t) = a (2 cos M(t-1) - M(t-2) + psi F);
@@ -14,11 +14,15 @@
 //   post_modal_kernel   recorder samples of step t + sums of the contraction
 //                       partials
 //   face2d_kernel       inverse 2D transforms -> pressure face layers
+//                       (face_gemm_kernel: two GEMM passes)
 //   iface_kernel        6th-order interface forcing into the force face
 //                       layers / PML strips (owner masks resolve overlapping
 //                       strips in the reference's list order)
 // The air partitions' kernels (face, modal, sums) launch once per air group
-// (up to two groups on two streams).
+// (up to two groups on two streams).  Every step kernel starts with
+// grid_dependency_wait: the host launches them with programmatic stream
+// serialization.  xform_gemm_kernel (register-staged GEMM) serves the dense
+// whole-field transforms of the readouts and the initial pressure.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -105,9 +109,11 @@ __device__ __forceinline__ T warp_sum(T v) {
 }
 
 // ---------------------------------------------------------------------------
-// Face transforms: every job is a small GEMM (see XformJob); one 64 x 64
-// output tile per block iteration, K staged through shared memory in chunks
-// of 16, 4 x 4 outputs per thread.
+// Batched 1D transforms as small GEMMs (see XformJob); one 64 x 64 output
+// tile per block iteration, K staged through registers and shared memory in
+// chunks of 16, 4 x 4 outputs per thread.  Used for the dense whole-field
+// transforms (readouts, initial pressure); the step's face passes use
+// face_gemm_kernel below.
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ int find_job(const XformJob* __restrict__ jobs, int njobs, int unit) {
