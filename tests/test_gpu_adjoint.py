@@ -194,12 +194,13 @@ def test_adjoint_errors():
 
 
 def test_adjoint_through_gemm_face_transforms():
-    """FP64 with 140-row faces (more than the fused face kernel's 128): the
-    face transforms (and their transposes) take the two-pass GEMM path;
-    source-series and face-scale gradients against central differences."""
+    """FP64 with faces of 139-141 rows (more than the fused face kernel's
+    128, not multiples of 4): the face transforms (and their transposes) take
+    the two-pass GEMM path with scalar staging; source-series and face-scale
+    gradients against central differences."""
     dh, c0 = 0.1, 343.0
     dt = 0.5 * dh / (c0 * np.sqrt(3.0))
-    air, srcs, recs = [(0, 0, 0, 140, 140, 16)], [(30, 40, 8)], [(60, 55, 8), (20, 80, 7)]
+    air, srcs, recs = [(0, 0, 0, 141, 139, 15)], [(30, 40, 7)], [(60, 55, 7), (20, 80, 6)]
     T = 60
     scene = A.build_scene(air, srcs, recs, dh, dt, c0, 5)
     sim = A.Simulation(scene, precision=A.PREC_F64, max_steps=T, adjoint=True)
