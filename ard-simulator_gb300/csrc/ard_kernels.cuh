@@ -571,6 +571,13 @@ __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
     return;
   }
   T* __restrict__ buf = a.buf;
+  // first elements of the jobs, cached for the per-element job search
+  constexpr int kMaxCachedJobs = 1024;
+  __shared__ long long sfirst[kMaxCachedJobs];
+  const bool cached = a.njobs <= kMaxCachedJobs;
+  if (cached)
+    for (int i = threadIdx.x; i < a.njobs; i += blockDim.x) sfirst[i] = a.jobs[i].first;
+  __syncthreads();
   const long long nb = (long long)gridDim.x - a.rec_blocks;
   for (long long g = ((long long)blockIdx.x - a.rec_blocks) * blockDim.x + threadIdx.x; g < a.total;
        g += nb * blockDim.x) {
@@ -578,7 +585,7 @@ __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
     int lo = 0, hi = a.njobs - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (a.jobs[mid].first <= gg) lo = mid; else hi = mid - 1;
+      if ((cached ? sfirst[mid] : a.jobs[mid].first) <= gg) lo = mid; else hi = mid - 1;
     }
     const SumJob J = a.jobs[lo];
     const T* p = buf + J.base + (gg - J.first);
@@ -1303,52 +1310,62 @@ __global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
     }
     const T r180 = (T)1 / ((T)180 * a.dh * a.dh), r12 = (T)1 / ((T)12 * a.dh), rdt = (T)1 / a.dt;
     // tiles of the next layer are fetched into registers while the current
-    // layer computes (3 + 2 + 2 values per thread, plus p(t-2) and the force)
+    // layer computes (3 + 2 + 2 values per thread, plus p(t-2) and the force);
+    // the in-layer offsets of a thread's tile elements (-1: outside the slab
+    // or the tile, read as zero) are the same for every layer
+    int oP[3], oA[2], oB[2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int i = threadIdx.x + 256 * k;
+      const int r = i / (TB + 6), c = i - r * (TB + 6);
+      const int aa = a0 + r - 3, bb = b0 + c - 3;
+      oP[k] = (i < (TA + 6) * (TB + 6) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? aa * B + bb : -1;
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int i = threadIdx.x + 256 * k;
+      const int r = i / TB, c = i - r * TB;
+      const int aa = a0 + r - 2, bb = b0 + c;
+      oA[k] = (i < (TA + 4) * TB && aa >= 0 && aa < A && bb < B) ? aa * B + bb : -1;
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int i = threadIdx.x + 256 * k;
+      const int r = i / (TB + 4), c = i - r * (TB + 4);
+      const int aa = a0 + r, bb = b0 + c - 2;
+      oB[k] = (i < TA * (TB + 4) && aa < A && bb >= 0 && bb < B) ? aa * B + bb : -1;
+    }
     T nP[3], nA[2], nB[2], nold = 0, nforce = 0;
     auto fetch = [&](int l) {
       const T* pl = p + l * lstride;
       const T* fal = fa + l * lstride;
       const T* fbl = fb + l * lstride;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const int i = threadIdx.x + 256 * k;
-        const int r = i / (TB + 6), c = i - r * (TB + 6);
-        const int aa = a0 + r - 3, bb = b0 + c - 3;
-        nP[k] = (i < (TA + 6) * (TB + 6) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? pl[(long long)aa * B + bb] : (T)0;
-      }
+      for (int k = 0; k < 3; ++k) nP[k] = oP[k] >= 0 ? pl[oP[k]] : (T)0;
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int i = threadIdx.x + 256 * k;
-        const int r = i / TB, c = i - r * TB;
-        const int aa = a0 + r - 2, bb = b0 + c;
-        nA[k] = (i < (TA + 4) * TB && aa >= 0 && aa < A && bb < B) ? fal[(long long)aa * B + bb] : (T)0;
-      }
+      for (int k = 0; k < 2; ++k) nA[k] = oA[k] >= 0 ? fal[oA[k]] : (T)0;
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int i = threadIdx.x + 256 * k;
-        const int r = i / (TB + 4), c = i - r * (TB + 4);
-        const int aa = a0 + r, bb = b0 + c - 2;
-        nB[k] = (i < TA * (TB + 4) && aa < A && bb >= 0 && bb < B) ? fbl[(long long)aa * B + bb] : (T)0;
-      }
+      for (int k = 0; k < 2; ++k) nB[k] = oB[k] >= 0 ? fbl[oB[k]] : (T)0;
       const int sl = l - P.strip0;
       nold = inside ? pn[l * lstride + col] : (T)0;
       nforce = (inside && sl >= 0 && sl < 3) ? force[sl * lstride + col] : (T)0;
     };
+    // the tiles as flat arrays: element i of a thread's k-th value
     auto commit = [&]() {
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const int i = threadIdx.x + 256 * k;
-        if (i < (TA + 6) * (TB + 6)) Ps[i / (TB + 6)][i % (TB + 6)] = nP[k];
+        if (i < (TA + 6) * (TB + 6)) (&Ps[0][0])[i] = nP[k];
       }
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         const int i = threadIdx.x + 256 * k;
-        if (i < (TA + 4) * TB) FA[i / TB][i % TB] = nA[k];
+        if (i < (TA + 4) * TB) (&FA[0][0])[i] = nA[k];
       }
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         const int i = threadIdx.x + 256 * k;
-        if (i < TA * (TB + 4)) FB[i / (TB + 4)][i % (TB + 4)] = nB[k];
+        if (i < TA * (TB + 4)) (&FB[0][0])[i] = nB[k];
       }
     };
     fetch(0);
