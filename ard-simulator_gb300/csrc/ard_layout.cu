@@ -749,6 +749,19 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
                        ctx->f2d_bytes <= (size_t)std::min(ctx->smem_optin, 200 * 1024);
   }
   if (ctx->adjoint) build_adjoint_jobs(ctx);
+  // every GEMM job list runs as one face_gemm_kernel instance: its jobs must
+  // agree on the pass direction, the table orientation and the input pair
+  {
+    const JobList* lists[] = {&ctx->fwd1, &ctx->fwd2, &ctx->inv1, &ctx->inv2,
+                              &ctx->adjg[0], &ctx->adjg[1], &ctx->adjg[2], &ctx->adjg[3]};
+    for (const JobList* L : lists)
+      for (const XformJob& j : L->jobs)
+        if (j.rows != L->jobs[0].rows || j.inverse != L->jobs[0].inverse ||
+            (j.in1 >= 0) != (L->jobs[0].in1 >= 0)) {
+          ctx->err = "internal: mixed GEMM job list";
+          return ARD_ERR_STATE;
+        }
+  }
   // ---- air partition groups: two streams in the step graph when the fused
   // face transforms are used and a split leaves each side >= 20 % of the cells ----
   ctx->ngroups = 1;
