@@ -1471,10 +1471,11 @@ __global__ void __launch_bounds__(256) iface_kernel(IfaceArgs<T> a) {
   for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < a.total;
        g += (long long)gridDim.x * blockDim.x) {
     const IfaceDev& I = a.ifs[a.cell_iface[g]];
-    const long long local = g - I.cell0;
+    const int local = (int)(g - I.cell0);   // cells of one interface: a face area, 32-bit
     const int nu = I.u1 - I.u0;
-    const int iu = I.u0 + (int)(local % nu);
-    const int iv = I.v0 + (int)(local / nu);
+    const int iv_l = local / nu;
+    const int iu = I.u0 + (local - iv_l * nu);
+    const int iv = I.v0 + iv_l;
     const unsigned mask = a.masks[I.mask + local];
     const int lu = iu - I.lo.ou, lv = iv - I.lo.ov;
     const int hu = iu - I.hi.ou, hv = iv - I.hi.ov;

@@ -602,6 +602,10 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         }
         ctx->masks.push_back(bits);
       }
+    if ((long long)(I.u1 - I.u0) * (I.v1 - I.v0) >= (1LL << 31)) {   // the interface kernel indexes cells in 32 bits
+      ctx->err = "interface with 2^31 or more face cells";
+      return ARD_ERR_RANGE;
+    }
     ctx->n_face_cells += (long long)(I.u1 - I.u0) * (I.v1 - I.v0);
     for (int side = 0; side < 2; ++side) {
       SideDev& S = side ? I.hi : I.lo;
