@@ -15,8 +15,11 @@ extra work, not counted.
           recorder history back
   roofline  the modal kernel (the dominant stage): algorithmic bytes per
           launch (28 B per air cell, the reference's per-cell reads and
-          writes of one air-partition update) over its CUDA-event time,
-          against the measured HBM copy bandwidth
+          writes of one air-partition update) over its CUDA-event time
+          (ard_profile_steps: the step's stages launched directly on one
+          stream, events around each stage, averaged over min(sim_steps,
+          200) steps in this process), against the measured HBM copy bandwidth; traffic = the
+          kernel's DRAM bytes per launch from the ncu summary in profiles/
   cpu_baseline  the oracle (C restatement of the reference's CPU solver,
           FP32, OpenMP over partitions) on a bounded sample of the same scene
   accuracy  FP32 recorders against the FP64 GPU path (same kernels in
@@ -24,8 +27,9 @@ extra work, not counted.
   adjoint the forward + adjoint of the recorder misfit on the same workload
           (gradients w.r.t. source series, initial pressure and the six PML
           face scales; target from a seeded perturbed source, face scales
-          U(0.5, 1.5), checkpoints every 64 steps): wall time against the
-          forward alone, and Gcell-steps/s of forward + adjoint
+          U(0.5, 1.5); --checkpoint-every K, 0 = the library's choice: the
+          whole PML history when it fits): wall time against the forward
+          alone, and Gcell-steps/s of forward + adjoint
   --plain runs every scene in its own context one after another (the
           per-scene path) instead of one batched context
 
