@@ -141,9 +141,11 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(cfg, sample_steps):
+def cpu_baseline(cfg, sample_steps, target_s=0.0):
     """The oracle (C restatement of the reference CPU solver, FP32) on the
-    first scene of the workload for `sample_steps` steps, all host threads."""
+    first scene of the workload, all host threads: at least `sample_steps`
+    steps, continued (in chunks of about a second) until `target_s` seconds
+    of stepping, within the scene's series length."""
     from oracle import oracle as O
     sc = cfg["scenes"][0]
     params = dict(dh=float(np.float32(cfg["h"])), dt=cfg["dt"], c0=float(np.float32(cfg["c0"])),
@@ -153,9 +155,15 @@ def cpu_baseline(cfg, sample_steps):
     for i, s in enumerate(sc["series"]):
         sim.set_source_series(i, s)
     sim.step(1)  # first-touch allocation outside the timing
+    limit = max(sample_steps, int(cfg["steps"]) - 1)
     t0 = time.perf_counter()
     sim.step(sample_steps)
     el = time.perf_counter() - t0
+    while el < target_s and sample_steps < limit:
+        chunk = max(1, min(limit - sample_steps, int(sample_steps / max(el, 1e-6))))
+        sim.step(chunk)
+        sample_steps += chunk
+        el = time.perf_counter() - t0
     n_air = sum(b[3] * b[4] * b[5] for b in sc["air"])
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return dict(value=n_air * sample_steps / el / 1e9, unit=UNIT, cores=cores, kind="port",
@@ -291,7 +299,9 @@ def main():
     ap.add_argument("--config", default="c1")
     ap.add_argument("--sim-steps", type=int, default=None, help="time steps per simulation (default: config)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample", type=int, default=10, help="time steps of the CPU baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=2, help="minimum time steps of the CPU baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="the CPU baseline steps on until this many seconds (within the series length)")
     ap.add_argument("--ref-sample", type=int, default=6, help="time steps per reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
@@ -503,7 +513,7 @@ def main():
         line["adjoint"] = adjoint_measurement(A, cfg, scenes, args, local)
     if rank == 0 and not args.no_cpu_baseline:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
-        line["cpu_baseline"] = cpu_baseline(cfg, args.cpu_sample)
+        line["cpu_baseline"] = cpu_baseline(cfg, args.cpu_sample, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     sim.close()
