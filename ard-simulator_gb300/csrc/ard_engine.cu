@@ -355,7 +355,7 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
         const int n = G.t_hi - G.t_lo;
         if (n > 0) {
           ModalArgs<T> ma{buf, ctx->d_dct, ctx->d_tiles + G.t_lo, n, ctx->d_srcpts, ctx->d_recpts,
-                          ctx->d_series, ctx->max_steps, ctx->d_t, tstep, par};
+                          ctx->d_series, ctx->max_steps, ctx->d_t, tstep, par, nullptr, 0};
           const int mgrid = grid_for(n, 1, ctx->num_sms * 2);
           if (ctx->arith == ARD_ARITH_REFERENCE)
             ARD_CUDA(launch_dep(modal_kernel<T, true, false>, mgrid, kModalThreads, msmem, st, ma));

@@ -75,7 +75,7 @@ struct Ctx {
   int ngroups = 1;
   AirGroup groups[2];
   bool fused_faces = false;
-  Face2DSmem f2d_smem{0, 0, 0};
+  Face2DSmem f2d_smem{0, 0, 0, 0};
   size_t f2d_bytes = 0;
   std::vector<std::pair<int, long long>> cos_tables;  // extent -> offset
   long long n_pml_cells = 0, n_face_cells = 0;

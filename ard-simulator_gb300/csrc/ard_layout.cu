@@ -501,7 +501,6 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         return ARD_ERR_INVALID;
       }
       const ard_partition& A = sc.partitions[b.a];
-      const ard_partition& B = sc.partitions[b.b];
       bool a_lo;
       int u0, u1, v0, v1;
       if (b.type == ARD_BOUNDARY_X) {
