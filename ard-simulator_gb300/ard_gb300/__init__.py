@@ -92,6 +92,8 @@ SIGNATURES = {
     "ard_create": (C.c_int, [C.POINTER(SceneDesc), C.c_int32, C.POINTER(Options), C.POINTER(C.c_void_p)]),
     "ard_destroy": (C.c_int, [C.c_void_p]),
     "ard_set_source_series": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float), C.c_int64]),
+    "ard_set_source_samples": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_int64,
+                                         C.POINTER(C.c_float)]),
     "ard_set_initial_pressure": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
     "ard_set_pml_scale": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
     "ard_reset": (C.c_int, [C.c_void_p]),
@@ -296,6 +298,13 @@ class Simulation:
     def set_source_series(self, source, series, scene=0):
         s = np.ascontiguousarray(series, np.float32)
         self._c(lib().ard_set_source_series(self._h, scene, source, _fptr(s), s.size))
+
+    def set_source_samples(self, t0, samples, source=-1, scene=-1):
+        """Samples t0 .. t0+n-1 of one source's series (source, scene >= 0:
+        `samples` is [n]) or of every source (-1, -1: [n_sources_total][n])."""
+        s = np.ascontiguousarray(samples, np.float32)
+        n = s.shape[-1] if s.ndim else 0
+        self._c(lib().ard_set_source_samples(self._h, scene, source, t0, n, _fptr(s)))
 
     def set_initial_pressure(self, partition, pressure, scene=0):
         p = np.ascontiguousarray(pressure, np.float32)

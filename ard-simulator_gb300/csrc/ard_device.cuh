@@ -163,4 +163,26 @@ struct Face2DJob {
   double scale;
 };
 
+// One batched product of the tensor-core face transforms (ard_mma.cuh): one
+// pass over the stacked layer outputs of one axis of one air partition,
+//   out[o][n][r] = scale * sum_k Data(o, r)[k] * Table[n][k],
+// data row m = o * R + r (output o, row r of it).
+constexpr int kMmaMaxOut = 6;
+
+struct MmaJob {
+  long long in0[kMmaMaxOut];   // data row r of output o: in0[o] + r * ldb  (+ sgn[o] * (in1[o] + r * ldb))
+  long long in1[kMmaMaxOut];   // -1: no second input
+  long long out[kMmaMaxOut];   // out[o] + n * ldo + r
+  long long thi, tlo;          // split table [N][tp]
+  int sgn[kMmaMaxOut];
+  int nout, R;                 // outputs, data rows per output
+  int K, N, tp;                // contraction length, output columns, table row pitch
+  int ldb, ldo;
+  int bn;                      // N tile width (multiple of 16, <= kMmaBNMax)
+  int mt, nt;                  // tiles along M (128 rows) and N
+  int first;                   // first tile of the job in its list
+  int vec;                     // data rows start on 16-byte boundaries (ldb and inputs multiples of 4)
+  float scale;
+};
+
 }  // namespace ard

@@ -19,6 +19,7 @@
 #include "ard_engine.h"
 #include "ard_gb300.h"
 #include "ard_kernels.cuh"
+#include "ard_mma.cuh"
 
 using namespace ard;
 
@@ -40,6 +41,13 @@ int grid_for(long long work, int per_block, int max_blocks) {
   if (b < 1) b = 1;
   if (b > max_blocks) b = max_blocks;
   return (int)b;
+}
+
+// One tensor-core face pass (job list k) on stream s: one CTA per SM at most.
+cudaError_t launch_mma(Ctx* ctx, int k, cudaStream_t s) {
+  if (ctx->mtiles[k] == 0) return cudaSuccess;
+  MmaArgs a{reinterpret_cast<float*>(ctx->d_buf), ctx->d_mjobs[k], (int)ctx->mjobs[k].size(), ctx->mtiles[k], ctx->d_err};
+  return launch_dep(face_mma_kernel, grid_for(ctx->mtiles[k], 1, ctx->num_sms), kMmaThreads, kMmaSmemBytes, s, a);
 }
 
 }  // namespace
@@ -107,6 +115,8 @@ static int configure_kernels(Ctx* ctx) {
       ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, f2d));
   }
   ARD_CUDA(ctx->prec == ARD_PREC_F64 ? configure_face_gemm<double>() : configure_face_gemm<float>());
+  if (ctx->mma_faces)
+    ARD_CUDA(cudaFuncSetAttribute(face_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMmaSmemBytes));
   return ARD_OK;
 }
 
@@ -131,6 +141,10 @@ extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_o
     const char* dbg = std::getenv("ARD_DEBUG_SYNC");
     ctx->debug_sync = dbg && dbg[0] == '1';
     if (ctx->debug_sync) ctx->use_graphs = false;
+    // ARD_FACE_TWO_PASS=1: the two-pass face transforms (tensor-core passes in
+    // FP32) even where the fused face kernel fits
+    const char* tp = std::getenv("ARD_FACE_TWO_PASS");
+    if (tp && tp[0] == '1') ctx->tune_gemm = 1;
   }
   if (ctx->arith != ARD_ARITH_ACCURATE && ctx->arith != ARD_ARITH_REFERENCE) {
     g_create_error = "ard_create: bad arithmetic mode";
@@ -155,7 +169,7 @@ extern "C" int ard_create(const ard_scene* scenes, int32_t n_scenes, const ard_o
   const bool autotune = opt && opt->autotune != 0;
   auto describe = [](const Ctx* c) {
     return std::string("tiles x") + std::to_string(c->tune_tiles) + ", lanes/row " +
-           (c->tune_g_shift == 0 ? "fit" : (c->tune_g_shift == 1 ? "narrow" : "narrower")) + ", faces " + (c->fused_faces ? "fused" : "gemm") + ", " +
+           (c->tune_g_shift == 0 ? "fit" : (c->tune_g_shift == 1 ? "narrow" : "narrower")) + ", faces " + (c->fused_faces ? "fused" : (c->mma_faces ? "tensor-core" : "gemm")) + ", " +
            std::to_string(c->tiles.size()) + " modal tiles, " + std::to_string(c->ngroups) + " air stream(s)";
   };
   if (!autotune) {
@@ -295,7 +309,7 @@ extern "C" int ard_synchronize(ard_ctx* c) {
   ARD_CUDA(cudaSetDevice(ctx->device));
   ARD_CUDA(cudaStreamSynchronize(ctx->stream));
   ARD_CUDA(cudaStreamSynchronize(ctx->stream2));
-  return ARD_OK;
+  return check_device_error(ctx);
 }
 
 // ---------------------------------------------------------------------------
@@ -343,12 +357,16 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
           if (n > 0)
             ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st, buf,
                                 ctx->d_fwd2d + G.f_lo, n, ctx->f2d_smem));
+        } else if (ctx->mma_faces) {
+          ARD_CUDA(launch_mma(ctx, 0, st));
         } else {
           ARD_CUDA(launch_face_gemm<T>(buf, ctx->fwd1.jobs[0], ctx->d_fwd1, (int)ctx->fwd1.jobs.size(), ctx->fwd1.units,
                                         grid_for(ctx->fwd1.units, 1, ctx->num_sms * 2), st));
         }
       } else if (k == kStageFwdCols) {
-        if (!ctx->fused_faces)
+        if (ctx->mma_faces)
+          ARD_CUDA(launch_mma(ctx, 1, st));
+        else if (!ctx->fused_faces)
           ARD_CUDA(launch_face_gemm<T>(buf, ctx->fwd2.jobs[0], ctx->d_fwd2, (int)ctx->fwd2.jobs.size(), ctx->fwd2.units,
                                         grid_for(ctx->fwd2.units, 1, ctx->num_sms * 2), st));
       } else if (k == kStageModal) {
@@ -370,12 +388,16 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
           if (n > 0)
             ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st, buf,
                                 ctx->d_inv2d + G.i_lo, n, ctx->f2d_smem));
+        } else if (ctx->mma_faces) {
+          ARD_CUDA(launch_mma(ctx, 2, st));
         } else {
           ARD_CUDA(launch_face_gemm<T>(buf, ctx->inv1.jobs[0], ctx->d_inv1, (int)ctx->inv1.jobs.size(), ctx->inv1.units,
                                         grid_for(ctx->inv1.units, 1, ctx->num_sms * 2), st));
         }
       } else if (k == kStageInvRows) {
-        if (!ctx->fused_faces)
+        if (ctx->mma_faces)
+          ARD_CUDA(launch_mma(ctx, 3, st));
+        else if (!ctx->fused_faces)
           ARD_CUDA(launch_face_gemm<T>(buf, ctx->inv2.jobs[0], ctx->d_inv2, (int)ctx->inv2.jobs.size(), ctx->inv2.units,
                                         grid_for(ctx->inv2.units, 1, ctx->num_sms * 2), st));
       }

@@ -75,6 +75,13 @@ struct Ctx {
   int ngroups = 1;
   AirGroup groups[2];
   bool fused_faces = false;
+  // Tensor-core face transforms (FP32 contexts whose faces take the two-pass
+  // form): the four passes as batched split-TF32 products (ard_mma.cuh), with
+  // the split transform tables of every extent in the pool.
+  bool mma_faces = false;
+  std::vector<MmaJob> mjobs[4];            // forward pass 1, 2; inverse pass 1, 2
+  int mtiles[4] = {0, 0, 0, 0};
+  std::vector<std::pair<int, long long>> mma_tables;   // extent -> offset of Chi, Clo, CiThi, CiTlo
   Face2DSmem f2d_smem{0, 0, 0, 0};
   size_t f2d_bytes = 0;
   std::vector<std::pair<int, long long>> cos_tables;  // extent -> offset
@@ -126,6 +133,8 @@ struct Ctx {
   XformJob* d_adjg[4] = {nullptr, nullptr, nullptr, nullptr};
   long long* d_tb = nullptr;      // adjoint counters {current step, first step of the PML history}
   void* d_phist = nullptr;        // PmlHist<T> read by the PML kernel (adjoint contexts only)
+  MmaJob* d_mjobs[4] = {nullptr, nullptr, nullptr, nullptr};
+  int* d_err = nullptr;           // set by a kernel whose bounded wait ran out (checked on synchronize)
 
   cudaStream_t stream = nullptr, stream2 = nullptr, stream3 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join3 = nullptr;
@@ -146,6 +155,7 @@ template <typename T>
 int launch_pml(Ctx* ctx, int par, int tstep, cudaStream_t s);
 int ensure_graph(Ctx* ctx);
 int check_guards(Ctx* ctx);
+int check_device_error(Ctx* ctx);
 template <typename T>
 int launch_post_modal(Ctx* ctx, cudaStream_t s, int tstep, bool with_recorders);
 template <typename T>

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -15,6 +16,7 @@
 #include "ard_engine.h"
 #include "ard_gb300.h"
 #include "ard_kernels.cuh"
+#include "ard_mma.cuh"
 
 using namespace ard;
 
@@ -245,6 +247,79 @@ void build_adjoint_jobs(Ctx* ctx) {
   }
 }
 
+// Job lists of the tensor-core face transforms (ard_mma.cuh) and the pool
+// space of their split tables.  Per air partition and axis (layer [V][ld],
+// transforms along U then V), with the transposed intermediate [6][U][Vp]
+// in the axis's tmp area (Vp = roundup(V, 4)):
+//   forward 1  X = f_n +/- f_{5-n}  [V][ld]   -> T^T [ku][v]   table C_U
+//   forward 2  T^T [ku][v]                    -> P  [kv][ku]   table C_V, scale s_f
+//   inverse 1  R = R_n +/- R_{3+n}  [kv][ld]  -> Y^T [u][kv]   table Ci_U^T
+//   inverse 2  Y^T [u][kv]                    -> p  [v][u]     table Ci_V^T, scale s_i
+// Outputs are stacked along the product's rows: forward o = pm 3 + n (the
+// even / odd parts of layer pair n), inverse o = layer L.
+template <typename Take>
+void build_mma_jobs(Ctx* ctx, Take take) {
+  std::map<int, long long> tab;
+  auto table = [&](int n) {
+    auto it = tab.find(n);
+    if (it != tab.end()) return it->second;
+    const long long tp = (n + 3) & ~3;
+    const long long o = take(4LL * n * tp);
+    tab[n] = o;
+    return o;
+  };
+  for (int k = 0; k < 4; ++k) { ctx->mjobs[k].clear(); ctx->mtiles[k] = 0; }
+  auto add = [&](int list, MmaJob j) {
+    const int nt = (j.N + kMmaBNMax - 1) / kMmaBNMax;
+    j.bn = ((j.N + nt - 1) / nt + 15) & ~15;
+    j.nt = (j.N + j.bn - 1) / j.bn;
+    j.mt = (j.nout * j.R + 127) / 128;
+    j.first = ctx->mtiles[list];
+    bool vec = j.ldb % 4 == 0;
+    for (int o = 0; o < j.nout; ++o) vec = vec && j.in0[o] % 4 == 0 && (j.in1[o] < 0 || j.in1[o] % 4 == 0);
+    j.vec = vec ? 1 : 0;
+    ctx->mtiles[list] += j.mt * j.nt;
+    ctx->mjobs[list].push_back(j);
+  };
+  for (const DctDev& D : ctx->dct) {
+    struct Axis { long long f, p, P, R, tmp; int nU, nV, ld; };
+    const Axis axes[3] = {{D.fX, D.pX, D.PX, D.RX, D.tmpX, D.h, D.d, D.h},
+                          {D.fY, D.pY, D.PY, D.RY, D.tmpY, D.w, D.d, D.wp},
+                          {D.fZ, D.pZ, D.PZ, D.RZ, D.tmpZ, D.w, D.h, D.wp}};
+    for (const Axis& a : axes) {
+      const long long LS = (long long)a.nV * a.ld;
+      const int Vp = (a.nV + 3) & ~3;
+      const long long TS = (long long)a.nU * Vp;   // one transposed intermediate
+      const long long tU = table(a.nU), tV = table(a.nV);
+      const long long tpU = (a.nU + 3) & ~3, tpV = (a.nV + 3) & ~3;
+      MmaJob f1{}, f2{}, i1{}, i2{};
+      f1.nout = f2.nout = i1.nout = i2.nout = 6;
+      for (int o = 0; o < 6; ++o) {
+        const int pm = o / 3, n = o % 3;
+        f1.in0[o] = a.f + n * LS; f1.in1[o] = a.f + (5 - n) * LS; f1.sgn[o] = pm ? -1 : 1;
+        f1.out[o] = a.tmp + o * TS;
+        f2.in0[o] = a.tmp + o * TS; f2.in1[o] = -1; f2.sgn[o] = 1;
+        f2.out[o] = a.P + o * LS;
+        const int L = o, nl = L < 3 ? L : 5 - L;
+        i1.in0[o] = a.R + nl * LS; i1.in1[o] = a.R + (3 + nl) * LS; i1.sgn[o] = L < 3 ? 1 : -1;
+        i1.out[o] = a.tmp + L * TS;
+        i2.in0[o] = a.tmp + L * TS; i2.in1[o] = -1; i2.sgn[o] = 1;
+        i2.out[o] = a.p + L * LS;
+      }
+      f1.R = a.nV; f1.ldb = a.ld; f1.K = f1.N = a.nU; f1.tp = (int)tpU; f1.thi = tU; f1.tlo = tU + a.nU * tpU;
+      f1.ldo = Vp; f1.scale = 1.f;
+      f2.R = a.nU; f2.ldb = Vp; f2.K = f2.N = a.nV; f2.tp = (int)tpV; f2.thi = tV; f2.tlo = tV + a.nV * tpV;
+      f2.ldo = a.ld; f2.scale = (float)D.sf;
+      i1.R = a.nV; i1.ldb = a.ld; i1.K = i1.N = a.nU; i1.tp = (int)tpU;
+      i1.thi = tU + 2 * a.nU * tpU; i1.tlo = tU + 3 * a.nU * tpU; i1.ldo = Vp; i1.scale = 1.f;
+      i2.R = a.nU; i2.ldb = Vp; i2.K = i2.N = a.nV; i2.tp = (int)tpV;
+      i2.thi = tV + 2 * a.nV * tpV; i2.tlo = tV + 3 * a.nV * tpV; i2.ldo = a.ld; i2.scale = (float)D.si;
+      add(0, f1); add(1, f2); add(2, i1); add(3, i2);
+    }
+  }
+  ctx->mma_tables.assign(tab.begin(), tab.end());
+}
+
 int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   const ard_scene& s0 = scenes[0];
   ctx->dh = s0.dh; ctx->dt = s0.dt; ctx->c0 = s0.c0;
@@ -452,7 +527,12 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     set_faces(D, pool.take(faces(D)), &D.pX, &D.pY, &D.pZ);
     D.PX = pool.take(FX); D.PY = pool.take(FY); D.PZ = pool.take(FZ);
     D.RX = pool.take(FX * D.nbx); D.RY = pool.take(FY * D.nby); D.RZ = pool.take(FZ * D.nbz);
-    D.tmpX = pool.take(FX); D.tmpY = pool.take(FY); D.tmpZ = pool.take(FZ);
+    // transform scratch: room for the [6][V][ld] GEMM intermediate and for the
+    // transposed [6][U][roundup(V, 4)] intermediate of the tensor-core passes
+    const int dp = (D.d + 3) & ~3, hp = (D.h + 3) & ~3;
+    D.tmpX = pool.take(std::max(FX, 6LL * D.h * dp));
+    D.tmpY = pool.take(std::max(FY, 6LL * D.w * dp));
+    D.tmpZ = pool.take(std::max(FZ, 6LL * D.w * hp));
     D.recpart = pool.take(std::max(1, D.nrec) * (long long)D.nbx * D.nby * D.nbz);
     D.srcpart = pool.take(std::max(1, D.nsrc) * (long long)D.nbx * D.nby * D.nbz);
   }
@@ -580,6 +660,10 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   }
   for (size_t i = 0; i < pend.size(); ++i) {
     IfaceDev I = pend[i].dev;
+    if ((long long)(I.u1 - I.u0) * (I.v1 - I.v0) >= (1LL << 31)) {   // the interface kernel indexes cells in 32 bits
+      ctx->err = "interface with 2^31 or more face cells";
+      return ARD_ERR_RANGE;
+    }
     I.mask = (long long)ctx->masks.size();
     I.cell0 = ctx->n_face_cells;
     for (int v = I.v0; v < I.v1; ++v)
@@ -601,10 +685,6 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         }
         ctx->masks.push_back(bits);
       }
-    if ((long long)(I.u1 - I.u0) * (I.v1 - I.v0) >= (1LL << 31)) {   // the interface kernel indexes cells in 32 bits
-      ctx->err = "interface with 2^31 or more face cells";
-      return ARD_ERR_RANGE;
-    }
     ctx->n_face_cells += (long long)(I.u1 - I.u0) * (I.v1 - I.v0);
     for (int side = 0; side < 2; ++side) {
       SideDev& S = side ? I.hi : I.lo;
@@ -765,6 +845,12 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
           return ARD_ERR_STATE;
         }
   }
+  // ---- tensor-core face transforms (FP32, two-pass form; ARD_FACE_MMA=0 keeps the CUDA-core passes) ----
+  {
+    const char* env = std::getenv("ARD_FACE_MMA");
+    ctx->mma_faces = ctx->prec == ARD_PREC_F32 && !ctx->fused_faces && !ctx->dct.empty() && !(env && env[0] == '0');
+    if (ctx->mma_faces) build_mma_jobs(ctx, [&](long long n) { return pool.take(n); });
+  }
   // ---- air partition groups: two streams in the step graph when the fused
   // face transforms are used and a split leaves each side >= 20 % of the cells ----
   ctx->ngroups = 1;
@@ -873,6 +959,10 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   if ((rc = up(&ctx->d_fwd2d, ctx->fwd2d))) return rc;
   if ((rc = up(&ctx->d_inv2d, ctx->inv2d))) return rc;
   if ((rc = up(&ctx->d_psum, ctx->psum))) return rc;
+  for (int k = 0; k < 4; ++k)
+    if (ctx->mma_faces && (rc = up(&ctx->d_mjobs[k], ctx->mjobs[k]))) return rc;
+  ARD_CUDA(cudaMalloc(&ctx->d_err, sizeof(int)));
+  ARD_CUDA(cudaMemset(ctx->d_err, 0, sizeof(int)));
   if (ctx->adjoint) {
     if ((rc = up(&ctx->d_adj1_2d, ctx->adj1_2d))) return rc;
     if ((rc = up(&ctx->d_adj2_2d, ctx->adj2_2d))) return rc;
@@ -895,6 +985,12 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     const int blocks = (int)std::min<long long>((nn + 255) / 256, 4096);
     if (ctx->prec == ARD_PREC_F64) cos_table_kernel<double><<<blocks, 256, 0, ctx->stream>>>((double*)ctx->d_buf, kv.second, kv.first);
     else cos_table_kernel<float><<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, kv.second, kv.first);
+    ARD_CUDA(cudaGetLastError());
+  }
+  for (auto& kv : ctx->mma_tables) {   // split TF32 tables of the tensor-core face passes (FP32 contexts)
+    const int n = kv.first, tp = (n + 3) & ~3;
+    const int blocks = (int)std::min<long long>(((long long)n * tp + 255) / 256, 4096);
+    mma_table_kernel<<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, kv.second, n, tp);
     ARD_CUDA(cudaGetLastError());
   }
   for (const DctDev& D : ctx->dct) {
@@ -931,7 +1027,8 @@ void free_ctx_device(Ctx* ctx) {
                   ctx->d_inv2d, ctx->d_series,
                   ctx->d_hist, ctx->d_t, ctx->d_adj1_2d, ctx->d_adj2_2d, ctx->d_adjg[0], ctx->d_adjg[1],
                   ctx->d_adjg[2], ctx->d_adjg[3], ctx->d_tb, ctx->d_phist, ctx->d_psum,
-                  ctx->d_cell_iface};
+                  ctx->d_cell_iface, ctx->d_mjobs[0], ctx->d_mjobs[1], ctx->d_mjobs[2], ctx->d_mjobs[3],
+                  ctx->d_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
@@ -1047,6 +1144,32 @@ extern "C" int ard_set_source_series(ard_ctx* c, int32_t scene, int32_t source, 
   return ARD_OK;
 }
 
+extern "C" int ard_set_source_samples(ard_ctx* c, int32_t scene, int32_t source, int64_t t0, int64_t n,
+                                      const float* samples) {
+  if (!c) return ARD_ERR_INVALID;
+  Ctx* ctx = as_ctx(c);
+  if (t0 < 0 || n < 0 || t0 + n > ctx->max_steps || (n > 0 && !samples)) {
+    ctx->err = "source samples outside [0, max_steps)";
+    return ARD_ERR_RANGE;
+  }
+  long long first = 0, count = 0;
+  if (scene == -1 && source == -1) {
+    count = ctx->n_src_total;   // samples is [n_sources_total][n]
+  } else {
+    if (scene < 0 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
+    const SceneRec& s = ctx->scenes[scene];
+    if (source < 0 || source >= s.nsrc) { ctx->err = "bad source index"; return ARD_ERR_RANGE; }
+    first = s.src0 + source;
+    count = 1;
+  }
+  if (n == 0 || count == 0) return ARD_OK;
+  ARD_CUDA(cudaSetDevice(ctx->device));
+  ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  ARD_CUDA(cudaMemcpy2D(ctx->d_series + first * ctx->max_steps + t0, sizeof(float) * ctx->max_steps, samples,
+                        sizeof(float) * n, sizeof(float) * n, (size_t)count, cudaMemcpyHostToDevice));
+  return ARD_OK;
+}
+
 extern "C" int ard_set_pml_scale(ard_ctx* c, int32_t scene, const float scale[6]) {
   if (!c || !scale) return ARD_ERR_INVALID;
   Ctx* ctx = as_ctx(c);
@@ -1119,6 +1242,7 @@ extern "C" int ard_read_recorders_f64(ard_ctx* c, int32_t scene, double* out, in
   if (nrec == 0 || nt == 0) return ARD_OK;
   ARD_CUDA(cudaSetDevice(ctx->device));
   ARD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (int rc = ard::check_device_error(ctx)) return rc;
   // rows of the history are n_rec_total wide; copy only this scene's columns
   ARD_CUDA(cudaMemcpy2D(out, sizeof(double) * nrec, ctx->d_hist + t0 * ctx->n_rec_total + rec0,
                         sizeof(double) * ctx->n_rec_total, sizeof(double) * nrec, nt, cudaMemcpyDeviceToHost));
@@ -1194,6 +1318,19 @@ extern "C" int ard_read_field(ard_ctx* c, int32_t scene, int32_t partition, floa
 }
 
 namespace ard {
+// The error word of the kernels with bounded waits (tensor-core face passes):
+// nonzero when one of them gave up.  Synchronous.
+int check_device_error(Ctx* ctx) {
+  if (!ctx->d_err) return ARD_OK;
+  int v = 0;
+  ARD_CUDA(cudaMemcpy(&v, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) {
+    ctx->err = "a tensor-core face transform gave up waiting for its MMAs (device error word set)";
+    return ARD_ERR_CUDA;
+  }
+  return ARD_OK;
+}
+
 // Checked mode: the guards around the pool must still hold their sentinel.
 int check_guards(Ctx* ctx) {
   if (!ctx->guard_bytes) return ARD_OK;

@@ -7,9 +7,10 @@
 // The readout is the inverse 3D transform of the partition's current modes
 // (REDFT01 on each axis, scaled by 1/sqrt(2N)), computed by the same GEMM
 // kernel as ard_read_field.  ard_read_field works through the context's own
-// scratch area; this variant keeps its intermediate in the file-scope array
-// g_field_scratch below, writes into the caller's device buffer and returns
-// without synchronising.
+// scratch area; this variant works entirely inside the file-scope array
+// g_field_scratch below (the unpadded modes, the three inverse tables and
+// both intermediates of the three passes), writes the caller's device buffer
+// only with the final copy, and returns without synchronising.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -24,17 +25,31 @@ using namespace ard;
 
 namespace {
 
-// Largest air partition the variant accepts: 4,194,304 cells.  The array
-// holds two such fields (32 MiB of device memory on every GPU that loads the
-// library, kept until the process exits).
+// Largest air partition the variant accepts: 4,194,304 cells, every extent
+// at most 1024.  The array holds two such fields and one 1024 x 1024 table
+// per axis: 44 MiB of device memory on every GPU that loads the library,
+// kept until the process exits.
 constexpr long long kNoAllocMaxCells = 1LL << 22;
-constexpr int kNoAllocMaxJobs = 1 + 1024 + 1;  // x pass, one y job per z-slice (depth <= 1024), z pass
+constexpr int kNoAllocMaxExtent = 1024;
+constexpr long long kNoAllocTable = (long long)kNoAllocMaxExtent * kNoAllocMaxExtent;
+constexpr int kNoAllocMaxJobs = 1 + kNoAllocMaxExtent + 1;  // x pass, one y job per z-slice, z pass
 
-static __device__ __align__(256) float g_field_scratch[2 * kNoAllocMaxCells];
+// element offsets inside the scratch array
+constexpr long long kFieldA = 0;
+constexpr long long kFieldB = kNoAllocMaxCells;
+constexpr long long kTabX = 2 * kNoAllocMaxCells;
+constexpr long long kTabY = kTabX + kNoAllocTable;
+constexpr long long kTabZ = kTabY + kNoAllocTable;
+constexpr long long kScratchElems = kTabZ + kNoAllocTable;
+
+static __device__ __align__(256) float g_field_scratch[kScratchElems];
 static __device__ __align__(256) XformJob g_field_jobs[kNoAllocMaxJobs];
 
-// Device addresses of the two arrays, looked up once per device (host code
-// must not use the array names as addresses: they are host-side stand-ins).
+// Device addresses of the two arrays, looked up once per device with that
+// device current (host code must not use the array names as addresses:
+// they are host-side stand-ins).  A cudaDeviceReset ends every context of
+// this library on that device and with them the addresses kept here; the
+// library is not used across a device reset.
 struct DeviceSetup {
   bool done = false;
   float* scratch = nullptr;
@@ -60,13 +75,12 @@ int setup_device(Ctx* ctx) {
 }
 
 // Fills the job table on the device: the three passes of the inverse
-// transform, with absolute element offsets (the GEMM kernel gets a null base).
-__global__ void build_jobs_kernel(XformJob* jobs, long long a, long long b, long long o, long long cw, long long ch,
-                                  long long cd, int w, int h, int d, double scale) {
+// transform, element offsets relative to the scratch array:
+// x pass A -> B, y pass (per z-slice) B -> A, z pass A -> B.
+__global__ void build_jobs_kernel(XformJob* jobs, int w, int h, int d, double scale) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const long long plane = (long long)h * w;
-  auto make = [&](long long in0, long long out, long long tab, int n, int batch, int ld, int rows, double sc,
-                  int first) {
+  auto make = [&](long long in0, long long out, long long tab, int n, int batch, int ld, int rows, double sc) {
     XformJob j{};
     j.in0 = in0; j.in1 = -1; j.sgn = 1;
     j.out = out; j.ctab = tab; j.n = n; j.batch = batch; j.ld = ld;
@@ -74,16 +88,16 @@ __global__ void build_jobs_kernel(XformJob* jobs, long long a, long long b, long
     const int Md = rows ? batch : n, Nd = rows ? n : batch;
     j.tn = (Nd + 63) / 64;
     j.ntiles = ((Md + 63) / 64) * j.tn;
-    j.first = first;
+    j.first = 0;
     return j;
   };
-  if (i == 0) jobs[0] = make(a, b, cw, w, d * h, w, 1, 1.0, 0);                     // along x
-  if (i < d) {                                                                      // along y, per z-slice
-    XformJob j = make(b + i * plane, o + i * plane, ch, h, w, w, 0, 1.0, 0);
+  if (i == 0) jobs[0] = make(kFieldA, kFieldB, kTabX, w, d * h, w, 1, 1.0);                 // along x
+  if (i < d) {                                                                             // along y, per z-slice
+    XformJob j = make(kFieldB + i * plane, kFieldA + i * plane, kTabY, h, w, w, 0, 1.0);
     j.first = i * j.ntiles;
     jobs[1 + i] = j;
   }
-  if (i == 0) jobs[1 + d] = make(o, a, cd, d, (int)plane, (int)plane, 0, scale, 0);  // along z
+  if (i == 0) jobs[1 + d] = make(kFieldA, kFieldB, kTabZ, d, (int)plane, (int)plane, 0, scale);  // along z
 }
 
 }  // namespace
@@ -91,6 +105,7 @@ __global__ void build_jobs_kernel(XformJob* jobs, long long a, long long b, long
 extern "C" int ard_read_field_noalloc(ard_ctx* c, int32_t scene, int32_t partition, float* out_device, void* stream) {
   if (!c || !out_device) return ARD_ERR_INVALID;
   Ctx* ctx = reinterpret_cast<Ctx*>(c);
+  // every argument check before any work is queued
   if (ctx->prec != ARD_PREC_F32) { ctx->err = "ard_read_field_noalloc: FP32 contexts only"; return ARD_ERR_INVALID; }
   if (scene < 0 || scene >= (int)ctx->scenes.size()) { ctx->err = "bad scene index"; return ARD_ERR_RANGE; }
   const SceneRec& sr = ctx->scenes[scene];
@@ -99,11 +114,13 @@ extern "C" int ard_read_field_noalloc(ard_ctx* c, int32_t scene, int32_t partiti
     ctx->err = "ard_read_field_noalloc: air partitions only";
     return ARD_ERR_INVALID;
   }
+  if ((uintptr_t)out_device % sizeof(float)) { ctx->err = "ard_read_field_noalloc: output not float-aligned"; return ARD_ERR_INVALID; }
   const DctDev& D = ctx->dct[sr.engine_idx[partition]];
   const long long N = (long long)D.w * D.h * D.d;
-  if (N > kNoAllocMaxCells || D.d > 1024) {
-    ctx->err = "ard_read_field_noalloc: partition of " + std::to_string(N) + " cells exceeds the limit of " +
-               std::to_string(kNoAllocMaxCells) + " cells (depth <= 1024)";
+  if (N > kNoAllocMaxCells || D.w > kNoAllocMaxExtent || D.h > kNoAllocMaxExtent || D.d > kNoAllocMaxExtent) {
+    ctx->err = "ard_read_field_noalloc: partition " + std::to_string(D.w) + " x " + std::to_string(D.h) + " x " +
+               std::to_string(D.d) + " exceeds the limit of " + std::to_string(kNoAllocMaxCells) +
+               " cells with every extent <= " + std::to_string(kNoAllocMaxExtent);
     return ARD_ERR_RANGE;
   }
   if (cudaSetDevice(ctx->device) != cudaSuccess) { ctx->err = "cudaSetDevice failed"; return ARD_ERR_CUDA; }
@@ -116,23 +133,20 @@ extern "C" int ard_read_field_noalloc(ard_ctx* c, int32_t scene, int32_t partiti
     e = cudaEventRecord(ctx->ev_fork, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ctx->ev_fork, 0);
   }
-  // absolute element offsets of the pieces (all 256-byte aligned)
-  float* pool = (float*)ctx->d_buf;
+  const float* pool = (const float*)ctx->d_buf;
   const int lvl = (int)((ctx->t_host - 1) & 1);
-  const long long a = (long long)((uintptr_t)S.scratch / sizeof(float));
-  const long long b = a + kNoAllocMaxCells;
-  const long long o = (long long)((uintptr_t)out_device / sizeof(float));
-  auto abs_off = [&](long long pool_off) { return (long long)((uintptr_t)(pool + pool_off) / sizeof(float)); };
-  const long long ciw = abs_off(D.cw + (long long)D.w * D.w);
-  const long long cih = abs_off(D.ch + (long long)D.h * D.h);
-  const long long cid = abs_off(D.cd + (long long)D.d * D.d);
-  if ((uintptr_t)out_device % sizeof(float)) { ctx->err = "output not float-aligned"; return ARD_ERR_INVALID; }
-  // the modes without the row padding -> first half of the scratch
+  // the modes without the row padding -> field A; the inverse (REDFT01) tables of the three extents
   if (e == cudaSuccess)
-    e = cudaMemcpy2DAsync(S.scratch, D.w * sizeof(float), pool + D.M[lvl], D.wp * sizeof(float), D.w * sizeof(float),
-                          (size_t)D.h * D.d, cudaMemcpyDeviceToDevice, s);
+    e = cudaMemcpy2DAsync(S.scratch + kFieldA, D.w * sizeof(float), pool + D.M[lvl], D.wp * sizeof(float),
+                          D.w * sizeof(float), (size_t)D.h * D.d, cudaMemcpyDeviceToDevice, s);
+  const long long tab_src[3] = {D.cw + (long long)D.w * D.w, D.ch + (long long)D.h * D.h, D.cd + (long long)D.d * D.d};
+  const long long tab_dst[3] = {kTabX, kTabY, kTabZ};
+  const long long tab_n[3] = {D.w, D.h, D.d};
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+    e = cudaMemcpyAsync(S.scratch + tab_dst[k], pool + tab_src[k], sizeof(float) * tab_n[k] * tab_n[k],
+                        cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) {
-    build_jobs_kernel<<<(D.d + 127) / 128, 128, 0, s>>>(S.jobs, a, b, o, ciw, cih, cid, D.w, D.h, D.d, D.si);
+    build_jobs_kernel<<<(D.d + 127) / 128, 128, 0, s>>>(S.jobs, D.w, D.h, D.d, D.si);
     e = cudaGetLastError();
   }
   const int gb = ctx->num_sms * 4;
@@ -142,13 +156,14 @@ extern "C" int ard_read_field_noalloc(ard_ctx* c, int32_t scene, int32_t partiti
   };
   const int tx = tiles(D.w, D.d * D.h, 1), ty = tiles(D.h, D.w, 0) * D.d, tz = tiles(D.d, D.h * D.w, 0);
   if (e == cudaSuccess) {
-    xform_gemm_kernel<float><<<std::min(gb, tx), 256, 0, s>>>(nullptr, S.jobs, 1, tx);
-    xform_gemm_kernel<float><<<std::min(gb, ty), 256, 0, s>>>(nullptr, S.jobs + 1, D.d, ty);
-    xform_gemm_kernel<float><<<std::min(gb, tz), 256, 0, s>>>(nullptr, S.jobs + 1 + D.d, 1, tz);
+    xform_gemm_kernel<float><<<std::min(gb, tx), 256, 0, s>>>(S.scratch, S.jobs, 1, tx);
+    xform_gemm_kernel<float><<<std::min(gb, ty), 256, 0, s>>>(S.scratch, S.jobs + 1, D.d, ty);
+    xform_gemm_kernel<float><<<std::min(gb, tz), 256, 0, s>>>(S.scratch, S.jobs + 1 + D.d, 1, tz);
     e = cudaGetLastError();
   }
-  // the z pass wrote the field into the first half of the scratch
-  if (e == cudaSuccess) e = cudaMemcpyAsync(out_device, S.scratch, N * sizeof(float), cudaMemcpyDeviceToDevice, s);
+  // the z pass wrote the field into field B
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out_device, S.scratch + kFieldB, N * sizeof(float), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess && s != ctx->stream) {
     e = cudaEventRecord(ctx->ev_join, s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0);

@@ -201,6 +201,16 @@ int ard_destroy(ard_ctx* ctx);
 int ard_set_source_series(ard_ctx* ctx, int32_t scene, int32_t source,
                           const float* series, int64_t n);
 
+/* Samples t0 .. t0+n-1 of the series of source `source` of scene `scene`;
+ * the other samples stay as they are (the streaming form of
+ * ard_set_source_series: a host that produces the source signal block by
+ * block uploads each block before the steps that inject it, as
+ * SoundSource::SampleValue (sound_source.h:18) is sampled step by step).
+ * t0 + n <= max_steps.  scene = source = -1 writes every source of every
+ * scene from samples[n_sources_total][n].  Synchronous. */
+int ard_set_source_samples(ard_ctx* ctx, int32_t scene, int32_t source, int64_t t0, int64_t n,
+                           const float* samples);
+
 /* Initial pressure of air partition `partition` (width*height*depth floats,
  * [z][y][x]).  Sets both modal time levels so that the partition starts at
  * rest with this pressure.  Only before the first step (or after reset). */
@@ -253,14 +263,17 @@ int ard_write_outputs(ard_ctx* ctx, int32_t scene, const char* dir, int64_t nt);
 /* No counterpart in the reference.  The field readout of ard_read_field for
  * an air partition of an FP32 context, for callers that cannot allocate
  * device memory: it allocates nothing.  The caller passes a device buffer of
- * width*height*depth floats ([z][y][x]); the intermediate of the transform
- * lives in a fixed device array inside the library (32 MiB, on every GPU that
- * loads the library, until exit), so partitions are limited to 4,194,304
- * cells and depth 1024 (ARD_ERR_RANGE beyond).  Asynchronous on `stream`
- * (NULL: the context's stream), ordered after work already queued on the
- * context.  The first call on a device looks up the array's device address
- * and should come before any stream capture.  Calls share the array: calls
- * whose work overlaps on the GPU race with each other. */
+ * width*height*depth floats ([z][y][x]), which receives only the finished
+ * field; the modes, the transform tables and both intermediates of the
+ * transform live in a fixed device array inside the library (44 MiB, on
+ * every GPU that loads the library, until exit), so partitions are limited
+ * to 4,194,304 cells with every extent at most 1024 (ARD_ERR_RANGE beyond,
+ * nothing queued or written).  Asynchronous on `stream` (NULL: the
+ * context's stream), ordered after work already queued on the context.  The
+ * first call on a device looks up the array's device address and should
+ * come before any stream capture.  Calls share the array and it keeps the
+ * last call's contents: calls whose work overlaps on the GPU race with each
+ * other. */
 int ard_read_field_noalloc(ard_ctx* ctx, int32_t scene, int32_t partition, float* out_device, void* stream);
 
 /* ---- adjoint (gradients of a recorder misfit) ---- */

@@ -13,7 +13,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
-REFDIR = "/root/reference/ARD-simulator-190113"
+# The reference sources: ARD_REFERENCE_DIR, else where this container mounts them.
+REFDIR = os.environ.get("ARD_REFERENCE_DIR", "/root/reference/ARD-simulator-190113")
 REF_BIN = os.path.join(HERE, "_ref", "ard_ref")
 
 _SOURCES = ["ard_oracle.c", "dct_fft.c"]

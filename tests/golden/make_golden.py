@@ -30,11 +30,12 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 sys.path.insert(0, os.path.join(REPO, "ard-simulator_gb300"))
 
+from oracle import build_oracle  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 from oracle import scene_oracle as SO  # noqa: E402
 from ard_gb300 import configs as K  # noqa: E402
 
-ASSETS = "/root/reference/ARD-simulator-190113/assets"
+ASSETS = os.path.join(build_oracle.REFDIR, "assets")   # the reference's scene files
 
 
 def params_for(h, c=343.0, pml=5):

@@ -344,10 +344,14 @@ def test_edge_cases_empty_and_ragged():
             assert rel_l2(got[:, r], want[:, r]) < F32_TOL, r
 
 
-def test_gemm_face_transforms_fp32_match_oracle():
+@pytest.mark.parametrize("path", ["tensor-core", "gemm"])
+def test_gemm_face_transforms_fp32_match_oracle(path, monkeypatch):
     """200 x 200 faces in FP32 exceed the fused kernel's 128 rows: the
-    two-pass GEMM face transforms run; FP32 against the FP64 C oracle within
-    the FP32 bar (recorders a few cells from the source, reached in time)."""
+    two-pass face transforms run, on the tensor cores (default) or on the
+    CUDA cores (ARD_FACE_MMA=0); FP32 against the FP64 C oracle within the
+    FP32 bar (recorders a few cells from the source, reached in time)."""
+    if path == "gemm":
+        monkeypatch.setenv("ARD_FACE_MMA", "0")
     dh, c0 = 0.1, 343.0
     dt = float(np.float32(0.5 * dh / (c0 * np.sqrt(3.0))))
     air, srcs, recs = [(0, 0, 0, 200, 200, 16)], [(60, 80, 8)], [(66, 82, 8), (55, 77, 7)]
@@ -359,7 +363,7 @@ def test_gemm_face_transforms_fp32_match_oracle():
     ref.step(T)
     want = ref.recorders()
     sim = A.Simulation(A.build_scene(air, srcs, recs, dh, dt, c0, 5), max_steps=T)
-    assert "gemm" in sim.layout
+    assert "faces " + path in sim.layout
     sim.set_source_series(0, series)
     sim.run(T)
     got = sim.recorders(f64=True)
