@@ -168,15 +168,33 @@ struct Face2DJob {
 //   out[o][n][r] = scale * sum_k Data(o, r)[k] * Table[n][k],
 // data row m = o * R + r (output o, row r of it).
 constexpr int kMmaMaxOut = 6;
+constexpr int kMmaBK = 32;       // K chunk: one 128-byte swizzle row of fp32 / tf32
+constexpr int kMmaBNMax = 160;   // widest N tile
+
+// N tiling of a transform of length n: nt tiles of bn rows (bn a multiple of
+// 16, at most kMmaBNMax).  The split tables are stored pre-tiled as
+// [nt][nch][bn][32] with nch = ceil(n / 32): each (N tile, K chunk) block is
+// the 128-byte-swizzled K-major image the tensor cores read, zero-padded.
+__host__ __device__ inline void mma_ntile(int n, int* nt, int* bn) {
+  const int t = (n + kMmaBNMax - 1) / kMmaBNMax;
+  const int b = ((n + t - 1) / t + 15) & ~15;
+  *bn = b;
+  *nt = (n + b - 1) / b;
+}
+__host__ __device__ inline long long mma_table_elems(int n) {
+  int nt, bn;
+  mma_ntile(n, &nt, &bn);
+  return (long long)nt * ((n + kMmaBK - 1) / kMmaBK) * bn * kMmaBK;
+}
 
 struct MmaJob {
   long long in0[kMmaMaxOut];   // data row r of output o: in0[o] + r * ldb  (+ sgn[o] * (in1[o] + r * ldb))
   long long in1[kMmaMaxOut];   // -1: no second input
   long long out[kMmaMaxOut];   // out[o] + n * ldo + r
-  long long thi, tlo;          // split table [N][tp]
+  long long thi, tlo;          // split table, pre-tiled [nt][nch][bn][32] (mma_ntile)
   int sgn[kMmaMaxOut];
   int nout, R;                 // outputs, data rows per output
-  int K, N, tp;                // contraction length, output columns, table row pitch
+  int K, N, nch;               // contraction length, output columns, K chunks
   int ldb, ldo;
   int bn;                      // N tile width (multiple of 16, <= kMmaBNMax)
   int mt, nt;                  // tiles along M (128 rows) and N

@@ -248,7 +248,7 @@ void build_adjoint_jobs(Ctx* ctx) {
 }
 
 // Job lists of the tensor-core face transforms (ard_mma.cuh) and the pool
-// space of their split tables.  Per air partition and axis (layer [V][ld],
+// space of their split, pre-tiled tables.  Per air partition and axis (layer [V][ld],
 // transforms along U then V), with the transposed intermediate [6][U][Vp]
 // in the axis's tmp area (Vp = roundup(V, 4)):
 //   forward 1  X = f_n +/- f_{5-n}  [V][ld]   -> T^T [ku][v]   table C_U
@@ -263,16 +263,14 @@ void build_mma_jobs(Ctx* ctx, Take take) {
   auto table = [&](int n) {
     auto it = tab.find(n);
     if (it != tab.end()) return it->second;
-    const long long tp = (n + 3) & ~3;
-    const long long o = take(4LL * n * tp);
+    const long long o = take(4LL * mma_table_elems(n));
     tab[n] = o;
     return o;
   };
   for (int k = 0; k < 4; ++k) { ctx->mjobs[k].clear(); ctx->mtiles[k] = 0; }
   auto add = [&](int list, MmaJob j) {
-    const int nt = (j.N + kMmaBNMax - 1) / kMmaBNMax;
-    j.bn = ((j.N + nt - 1) / nt + 15) & ~15;
-    j.nt = (j.N + j.bn - 1) / j.bn;
+    mma_ntile(j.N, &j.nt, &j.bn);
+    j.nch = (j.K + kMmaBK - 1) / kMmaBK;
     j.mt = (j.nout * j.R + 127) / 128;
     j.first = ctx->mtiles[list];
     bool vec = j.ldb % 4 == 0;
@@ -291,7 +289,7 @@ void build_mma_jobs(Ctx* ctx, Take take) {
       const int Vp = (a.nV + 3) & ~3;
       const long long TS = (long long)a.nU * Vp;   // one transposed intermediate
       const long long tU = table(a.nU), tV = table(a.nV);
-      const long long tpU = (a.nU + 3) & ~3, tpV = (a.nV + 3) & ~3;
+      const long long SU = mma_table_elems(a.nU), SV = mma_table_elems(a.nV);   // Chi, Clo, CiThi, CiTlo each
       MmaJob f1{}, f2{}, i1{}, i2{};
       f1.nout = f2.nout = i1.nout = i2.nout = 6;
       for (int o = 0; o < 6; ++o) {
@@ -306,14 +304,14 @@ void build_mma_jobs(Ctx* ctx, Take take) {
         i2.in0[o] = a.tmp + L * TS; i2.in1[o] = -1; i2.sgn[o] = 1;
         i2.out[o] = a.p + L * LS;
       }
-      f1.R = a.nV; f1.ldb = a.ld; f1.K = f1.N = a.nU; f1.tp = (int)tpU; f1.thi = tU; f1.tlo = tU + a.nU * tpU;
+      f1.R = a.nV; f1.ldb = a.ld; f1.K = f1.N = a.nU; f1.thi = tU; f1.tlo = tU + SU;
       f1.ldo = Vp; f1.scale = 1.f;
-      f2.R = a.nU; f2.ldb = Vp; f2.K = f2.N = a.nV; f2.tp = (int)tpV; f2.thi = tV; f2.tlo = tV + a.nV * tpV;
+      f2.R = a.nU; f2.ldb = Vp; f2.K = f2.N = a.nV; f2.thi = tV; f2.tlo = tV + SV;
       f2.ldo = a.ld; f2.scale = (float)D.sf;
-      i1.R = a.nV; i1.ldb = a.ld; i1.K = i1.N = a.nU; i1.tp = (int)tpU;
-      i1.thi = tU + 2 * a.nU * tpU; i1.tlo = tU + 3 * a.nU * tpU; i1.ldo = Vp; i1.scale = 1.f;
-      i2.R = a.nU; i2.ldb = Vp; i2.K = i2.N = a.nV; i2.tp = (int)tpV;
-      i2.thi = tV + 2 * a.nV * tpV; i2.tlo = tV + 3 * a.nV * tpV; i2.ldo = a.ld; i2.scale = (float)D.si;
+      i1.R = a.nV; i1.ldb = a.ld; i1.K = i1.N = a.nU; i1.thi = tU + 2 * SU; i1.tlo = tU + 3 * SU;
+      i1.ldo = Vp; i1.scale = 1.f;
+      i2.R = a.nU; i2.ldb = Vp; i2.K = i2.N = a.nV; i2.thi = tV + 2 * SV; i2.tlo = tV + 3 * SV;
+      i2.ldo = a.ld; i2.scale = (float)D.si;
       add(0, f1); add(1, f2); add(2, i1); add(3, i2);
     }
   }
@@ -988,9 +986,9 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     ARD_CUDA(cudaGetLastError());
   }
   for (auto& kv : ctx->mma_tables) {   // split TF32 tables of the tensor-core face passes (FP32 contexts)
-    const int n = kv.first, tp = (n + 3) & ~3;
-    const int blocks = (int)std::min<long long>(((long long)n * tp + 255) / 256, 4096);
-    mma_table_kernel<<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, kv.second, n, tp);
+    const int n = kv.first;
+    const int blocks = (int)std::min<long long>((mma_table_elems(n) + 255) / 256, 4096);
+    mma_table_kernel<<<blocks, 256, 0, ctx->stream>>>((float*)ctx->d_buf, kv.second, n);
     ARD_CUDA(cudaGetLastError());
   }
   for (const DctDev& D : ctx->dct) {
