@@ -109,6 +109,14 @@ SIGNATURES = {
     "ard_read_initial_pressure_grad": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
     "ard_kernels_per_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ard_write_outputs": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.c_int64]),
+    "ard_record_neighbourhoods": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ard_read_neighbourhoods": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.c_int64, C.c_int64]),
+    "ard_slice_size": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "ard_render_slice": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_void_p,
+                                   C.c_void_p]),
+    "ard_impulse_response": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int64,
+                                       C.c_double, C.c_double, C.c_int32, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]),
     "ard_describe": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     "ard_profile_steps": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "ard_last_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
@@ -400,8 +408,60 @@ class Simulation:
         self._c(lib().ard_read_initial_pressure_grad(self._h, scene, partition, _fptr(out)))
         return out
 
+    def record_neighbourhoods(self, enable=True):
+        """Record the 10x10x10 pressure cube around every recorder after every
+        following step (Recorder::RecordField's out_ stream; ard_record_neighbourhoods)."""
+        self._c(lib().ard_record_neighbourhoods(self._h, 1 if enable else 0))
+
+    def neighbourhoods(self, scene=0, t0=0, nt=None):
+        """Recorded cubes [nt][n_recorders][10][10][10] ([z][y][x] offsets -5 .. 4)."""
+        nt = self.time_step - t0 if nt is None else nt
+        nrec = (sum(s.desc.n_recorders for s in self.scenes) if scene == -1
+                else self.scenes[scene].desc.n_recorders)
+        out = np.zeros((nt, nrec, 10, 10, 10), np.float32)
+        self._c(lib().ard_read_neighbourhoods(self._h, scene, _fptr(out), t0, nt))
+        return out
+
+    def slice_size(self, look_from=0, scene=0):
+        w, h = C.c_int32(), C.c_int32()
+        self._c(lib().ard_slice_size(self._h, scene, look_from, C.byref(w), C.byref(h)))
+        return w.value, h.value
+
+    def render_slice(self, look_from=0, coord=None, v_coef=10.0, scene=0, pixels=None, pressure=None):
+        """Colour map of a pressure slice (Simulation::Update's visualization,
+        ard_render_slice) into device buffers: `pixels` an int32 CUDA tensor of
+        [height][width] RGBA8888 words (allocated zeroed when None), `pressure`
+        an optional float32 CUDA tensor of the same shape.  coord defaults to
+        the first source's z (xy) or x (yz), as the reference takes it."""
+        import torch
+        w, h = self.slice_size(look_from, scene)
+        if coord is None:
+            src = self.scenes[scene].sources[0]
+            coord = src[2] if look_from == 0 else src[0]
+        dev = torch.device("cuda", torch.cuda.current_device())
+        if pixels is None:
+            pixels = torch.zeros((h, w), dtype=torch.int32, device=dev)
+        self._c(lib().ard_render_slice(self._h, scene, look_from, int(coord), float(v_coef),
+                                       C.c_void_p(pixels.data_ptr()),
+                                       C.c_void_p(pressure.data_ptr()) if pressure is not None else None))
+        return pixels
+
+    def impulse_response(self, nt=None, recorder=0, source=0, scene=0, truncate=0, sample_rate=0.0, fcut=3000.0,
+                         fir_order=1024):
+        """Room impulse response and T60 of matlab/auralization.m and t60.m on
+        the device (ard_impulse_response).  Returns (rir [nt] float64,
+        dict(t60_ms, slope, stop, overrun))."""
+        nt = self.time_step if nt is None else nt
+        rir = np.zeros(nt, np.float64)
+        t60 = np.zeros(4, np.float64)
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self._c(lib().ard_impulse_response(self._h, scene, recorder, source, nt, truncate, sample_rate, fcut,
+                                           fir_order, dp(rir), dp(t60)))
+        return rir, dict(t60_ms=float(t60[0]), slope=float(t60[1]), stop=int(t60[2]), overrun=bool(t60[3]))
+
     def write_outputs(self, directory, scene=0, nt=None):
-        """response_<r>.txt and source_<s>.txt in the reference's format (ard_write_outputs)."""
+        """response_<r>.txt and source_<s>.txt in the reference's format, and
+        out_<r>.txt when the neighbourhoods are recorded (ard_write_outputs)."""
         nt = self.time_step if nt is None else nt
         self._c(lib().ard_write_outputs(self._h, scene, os.fsencode(directory), nt))
 

@@ -18,7 +18,7 @@ BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libard_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["ard_engine.cu", "ard_layout.cu", "ard_adjoint.cu", "ard_noalloc.cu", "ard_output.cu"]
+CU_SOURCES = ["ard_engine.cu", "ard_layout.cu", "ard_adjoint.cu", "ard_noalloc.cu", "ard_output.cu", "ard_post.cu"]
 CPP_SOURCES = ["ard_scene.cpp"]
 
 

@@ -26,15 +26,6 @@
 
 using namespace ard;
 
-#define ARD_CUDA(call)                                                                                   \
-  do {                                                                                                   \
-    cudaError_t e_ = (call);                                                                             \
-    if (e_ != cudaSuccess) {                                                                             \
-      ctx->err = std::string(#call) + ": " + cudaGetErrorName(e_) + " (" + cudaGetErrorString(e_) + ")"; \
-      return e_ == cudaErrorMemoryAllocation ? ARD_ERR_OOM : ARD_ERR_CUDA;                               \
-    }                                                                                                    \
-  } while (0)
-
 namespace {
 
 int grid_for(long long work, int per_block, int max_blocks) {

@@ -27,15 +27,6 @@ namespace {
 
 thread_local std::string g_create_error;
 
-#define ARD_CUDA(call)                                                                          \
-  do {                                                                                          \
-    cudaError_t e_ = (call);                                                                    \
-    if (e_ != cudaSuccess) {                                                                    \
-      ctx->err = std::string(#call) + ": " + cudaGetErrorName(e_) + " (" + cudaGetErrorString(e_) + ")"; \
-      return e_ == cudaErrorMemoryAllocation ? ARD_ERR_OOM : ARD_ERR_CUDA;                      \
-    }                                                                                           \
-  } while (0)
-
 int grid_for(long long work, int per_block, int max_blocks) {
   long long b = (work + per_block - 1) / per_block;
   if (b < 1) b = 1;
@@ -291,6 +282,7 @@ extern "C" int ard_kernels_per_step(const ard_ctx* c, int32_t* out) {
     else n += 4;
     n += G.t_hi > G.t_lo ? 1 : 0;                                                       // modal update
     n += (G.r_hi > G.r_lo || G.s_total > 0) ? 1 : 0;                                    // recorder + partial sums
+    n += (ctx->d_cube_hist && G.r_hi > G.r_lo) ? 3 : 0;                                  // recorder neighbourhoods
   }
   n += ctx->n_face_cells > 0 ? 1 : 0;        // interfaces
   *out = n;
@@ -381,7 +373,9 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
             ARD_CUDA(launch_dep(modal_kernel<T, false, false>, mgrid, kModalThreads, msmem, st, ma));
         }
       } else if (k == kStageRecorder) {
-        return launch_post_modal_range<T>(ctx, st, tstep, G.r_lo, G.r_hi, G.s_lo, G.s_hi, G.s_first, G.s_total);
+        if (int rc = launch_post_modal_range<T>(ctx, st, tstep, G.r_lo, G.r_hi, G.s_lo, G.s_hi, G.s_first, G.s_total))
+          return rc;
+        return launch_cubes<T>(ctx, st, tstep, par, G.r_lo, G.r_hi);
       } else if (k == kStageInvCols) {
         if (ctx->fused_faces) {
           const int n = G.i_hi - G.i_lo;

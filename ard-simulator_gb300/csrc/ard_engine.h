@@ -12,6 +12,18 @@
 #include "ard_gb300.h"
 #include "ard_kernels.cuh"
 
+// Host: a CUDA runtime call inside an entry point with a Ctx* named ctx;
+// a failure records the call and the CUDA error on the context and returns
+// ARD_ERR_OOM (allocation) or ARD_ERR_CUDA.
+#define ARD_CUDA(call)                                                                                   \
+  do {                                                                                                   \
+    cudaError_t e_ = (call);                                                                             \
+    if (e_ != cudaSuccess) {                                                                             \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorName(e_) + " (" + cudaGetErrorString(e_) + ")"; \
+      return e_ == cudaErrorMemoryAllocation ? ARD_ERR_OOM : ARD_ERR_CUDA;                               \
+    }                                                                                                    \
+  } while (0)
+
 namespace ard {
 
 struct JobList {
@@ -136,6 +148,14 @@ struct Ctx {
   MmaJob* d_mjobs[4] = {nullptr, nullptr, nullptr, nullptr};
   int* d_err = nullptr;           // set by a kernel whose bounded wait ran out (checked on synchronize)
 
+  // neighbourhood recording (ard_record_neighbourhoods): the 10 x 10 x 10
+  // pressure cube around every recorder after every step, [max_steps][n_rec_total][1000]
+  float* d_cube_hist = nullptr;
+  void* d_cube_tmp = nullptr;     // contraction scratch (T): per recorder T1 [d][h][10], T2 [d][100]
+  long long cube_s1 = 0, cube_s2 = 0;
+  int cube_row_blocks = 0, cube_dmax = 0;
+  long long cube_t0 = 0;          // first step whose cube is recorded
+
   cudaStream_t stream = nullptr, stream2 = nullptr, stream3 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join3 = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -167,5 +187,8 @@ template <typename T>
 int dense_transform_ex(Ctx* ctx, const DctDev& D, long long in, long long out, long long scratch, int which,
                        bool transpose, double scale);
 size_t elem_size(const Ctx* ctx);
+template <typename T>
+int launch_cubes(Ctx* ctx, cudaStream_t s, int tstep, int par, int r_lo, int r_hi);
+void free_cubes(Ctx* ctx);
 
 }  // namespace ard

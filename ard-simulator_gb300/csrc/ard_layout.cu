@@ -20,15 +20,6 @@
 
 using namespace ard;
 
-#define ARD_CUDA(call)                                                                                   \
-  do {                                                                                                   \
-    cudaError_t e_ = (call);                                                                             \
-    if (e_ != cudaSuccess) {                                                                             \
-      ctx->err = std::string(#call) + ": " + cudaGetErrorName(e_) + " (" + cudaGetErrorString(e_) + ")"; \
-      return e_ == cudaErrorMemoryAllocation ? ARD_ERR_OOM : ARD_ERR_CUDA;                               \
-    }                                                                                                    \
-  } while (0)
-
 namespace ard {
 
 size_t elem_size(const Ctx* ctx) { return ctx->prec == ARD_PREC_F64 ? sizeof(double) : sizeof(float); }
@@ -1020,6 +1011,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
 
 void free_ctx_device(Ctx* ctx) {
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  free_cubes(ctx);
   void* ptrs[] = {ctx->d_buf_base, ctx->d_mask, ctx->d_dct, ctx->d_pml, ctx->d_pml_blocks, ctx->d_ifs, ctx->d_srcpts,
                   ctx->d_recpts, ctx->d_tiles, ctx->d_fwd1, ctx->d_fwd2, ctx->d_inv1, ctx->d_inv2, ctx->d_fwd2d,
                   ctx->d_inv2d, ctx->d_series,
@@ -1184,6 +1176,7 @@ extern "C" int ard_reset(ard_ctx* c) {
   ARD_CUDA(cudaSetDevice(ctx->device));
   int rc = ard::zero_state(ctx);
   if (rc) return rc;
+  ctx->cube_t0 = 0;   // neighbourhood rows are recorded again from step 0
   ARD_CUDA(cudaStreamSynchronize(ctx->stream));
   return ARD_OK;
 }

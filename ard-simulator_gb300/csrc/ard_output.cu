@@ -1,9 +1,11 @@
 // Text output in the reference's formats (ARD-simulator-190113/output/README.md):
 // response_<i>.txt (Recorder::RecordField's response stream, recorder.cpp:
 // 15-16,55) and source_<i>.txt (SoundSource::RecordSource, sound_source.cpp:
-// 14-15,50-56): one value per line, written as an ostream writes a float
+// 14-15,50-56): one value per line; out_<i>.txt (Recorder::RecordField's
+// output stream, recorder.cpp:13-14,44-53): one line of the 10x10x10
+// neighbourhood per step.  Values are written as an ostream writes a float
 // (6 significant digits).  Host code over the context's recorded history and
-// source series; nothing here runs on the GPU besides the two copies.
+// source series; nothing here runs on the GPU besides the copies.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -43,6 +45,28 @@ extern "C" int ard_write_outputs(ard_ctx* c, int32_t scene, const char* dir, int
       std::vector<float> v((size_t)nt);
       for (int64_t t = 0; t < nt; ++t) v[t] = (float)h[(size_t)t * ctx->n_rec_total + sr.rec0 + r];
       if (!write("response_" + std::to_string(r) + ".txt", v)) { ctx->err = "ard_write_outputs: cannot write in " + std::string(dir); return ARD_ERR_INVALID; }
+    }
+  }
+  // neighbourhoods (recorded from step 0): one line of 1000 values per step,
+  // each followed by a space (recorder.cpp:44-53)
+  if (ctx->d_cube_hist && ctx->cube_t0 == 0 && sr.nrec > 0 && nt > 0) {
+    const size_t cells = 1000;
+    std::vector<float> cube((size_t)nt * cells);
+    for (int r = 0; r < sr.nrec; ++r) {
+      if (cudaMemcpy2D(cube.data(), sizeof(float) * cells, ctx->d_cube_hist + (size_t)(sr.rec0 + r) * cells,
+                       sizeof(float) * cells * ctx->n_rec_total, sizeof(float) * cells, nt,
+                       cudaMemcpyDeviceToHost) != cudaSuccess) {
+        ctx->err = "ard_write_outputs: neighbourhood copy failed";
+        return ARD_ERR_CUDA;
+      }
+      std::ofstream f(std::string(dir) + "/out_" + std::to_string(r) + ".txt", std::ios::out);
+      if (!f) { ctx->err = "ard_write_outputs: cannot write in " + std::string(dir); return ARD_ERR_INVALID; }
+      for (int64_t t = 0; t < nt; ++t) {
+        const float* row = cube.data() + (size_t)t * cells;
+        for (size_t k = 0; k < cells; ++k) f << row[k] << ' ';
+        f << '\n';
+      }
+      if (!f) { ctx->err = "ard_write_outputs: cannot write in " + std::string(dir); return ARD_ERR_INVALID; }
     }
   }
   // sources: the series as injected, [source][max_steps] (float)

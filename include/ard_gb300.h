@@ -256,9 +256,73 @@ int ard_read_field(ard_ctx* ctx, int32_t scene, int32_t partition, float* out);
  * 0 .. nt-1, one value per line, as Recorder::RecordField's response stream,
  * recorder.cpp:15-16,55) and source_<s>.txt per source (the injected series,
  * as SoundSource::RecordSource, sound_source.cpp:50-56), in directory `dir`
- * (which must exist).  The per-step 10x10x10 neighbourhood file out_<r>.txt
- * is not produced.  Synchronous. */
+ * (which must exist).  When the neighbourhoods were recorded from step 0
+ * (ard_record_neighbourhoods), also out_<r>.txt per recorder: one line per
+ * step with the 1000 values of the 10x10x10 cube, each followed by a space,
+ * as Recorder::RecordField's output stream (recorder.cpp:13-14,44-53).
+ * Synchronous. */
 int ard_write_outputs(ard_ctx* ctx, int32_t scene, const char* dir, int64_t nt);
+
+/* Recorder::RecordField's neighbourhood stream (recorder.cpp:40-57): with
+ * enable != 0 every following step also records, for every recorder of every
+ * scene, the pressure of the 10x10x10 cube of cells (x+k, y+j, z+i),
+ * i, j, k = -5 .. 4, after the step's update, kept on the device for
+ * max_steps steps (max_steps * n_recorders * 4000 bytes, allocated here).
+ * The cube is contracted from the partition's modes, three extra launches
+ * per step inside the step graph.  Every recorder's cube must lie inside its
+ * partition (Recorder::FindPartition's margin), else ARD_ERR_INVALID.
+ * enable = 0 frees the history.  Synchronous. */
+int ard_record_neighbourhoods(ard_ctx* ctx, int32_t enable);
+
+/* Recorded neighbourhoods of steps t0 .. t0+nt-1 of scene `scene` (-1: all
+ * scenes), as out[t][recorder][1000] with the cube in the reference's order
+ * (z offset slowest, x offset fastest).  Steps before the recording was
+ * enabled (or before the last ard_reset) are ARD_ERR_RANGE.  Synchronous. */
+int ard_read_neighbourhoods(ard_ctx* ctx, int32_t scene, float* out, int64_t t0, int64_t nt);
+
+/* Size of scene `scene`'s visualization image (Simulation::Simulation's
+ * size_x_ / size_y_ / size_z_, simulation.cpp:272-288: the bounding box of
+ * all partitions, PMLs included): look_from 0 (xy) gives size_x x size_y,
+ * look_from 1 (yz) size_y x size_z (width = row length). */
+int ard_slice_size(ard_ctx* ctx, int32_t scene, int32_t look_from, int32_t* width, int32_t* height);
+
+/* Headless form of Simulation::Update's visualization block
+ * (simulation.cpp:320-420): the colour map of a pressure slice into the
+ * caller's device buffer of width*height RGBA8888 words (ard_slice_size).
+ * look_from 0: the xy plane, 1: the yz plane; `coord` is the reference's
+ * pixels_z / pixels_x (the first source's z or x).  As the reference does,
+ * every partition (air and PML, in list order, later ones overwriting
+ * earlier ones) whose extent along the view axis reaches coord (end
+ * inclusive) is drawn, and coord is passed to it as a local coordinate;
+ * values outside the partition read 0 (PmlPartition::GetIndex's sentinel;
+ * the reference's air partitions read outside their array there).  Colour:
+ * norm = 0.5 clamp(p v_coef, -1, 1) + 0.5 (v_coef = 10 in the reference),
+ * word SDL_MapRGBA(RGBA8888, 255, r, g, b) = 0xFF000000 | r<<16 | g<<8 | b.
+ * Pixels no partition covers are left as they are.  pressure_device (may be
+ * NULL) receives the drawn pressure values in the same layout.
+ * Synchronous. */
+int ard_render_slice(ard_ctx* ctx, int32_t scene, int32_t look_from, int32_t coord, float v_coef,
+                     uint32_t* pixels_device, float* pressure_device);
+
+/* Room impulse response and reverberation time of matlab/auralization.m
+ * (:22-36) and matlab/t60.m, in FP64 on the device over the recorded
+ * pressure of recorder `recorder` and the injected series of source
+ * `source` of scene `scene`, steps 0 .. nt-1:
+ *   rr = response, zeroed from sample `truncate` on (truncate <= 0: kept
+ *        whole; auralization.m:25-27 truncates at its Sabine estimate);
+ *   rir = the first nt samples of xcorr(rr, reversed source)
+ *        (= the causal convolution of rr with the source), low-passed by
+ *        fftfilt(fir1(fir_order, fcut / (sr / 2)), .), divided by its
+ *        largest magnitude (normalizeIR.m);
+ *   t60 = Schroeder integration and the line fit of t60.m on rir.
+ * sample_rate <= 0 takes 1 / dt.  rir_out (nt doubles, may be NULL);
+ * t60_out (4 doubles, may be NULL): T60 in ms rounded as t60.m returns it,
+ * the fitted slope (dB/ms), the fit length `stop`, and 1 when t60.m's
+ * window would have been overrun (stop clamped to the window; 0 otherwise).
+ * Synchronous. */
+int ard_impulse_response(ard_ctx* ctx, int32_t scene, int32_t recorder, int32_t source, int64_t nt,
+                         int64_t truncate, double sample_rate, double fcut, int32_t fir_order,
+                         double* rir_out, double* t60_out);
 
 /* No counterpart in the reference.  The field readout of ard_read_field for
  * an air partition of an FP32 context, for callers that cannot allocate
