@@ -12,9 +12,10 @@ scenes and on the c0 / c1 benchmark scenes, and writes:
                      recorded), and the scene definition
 
 Usage (needs the reference sources on this machine):
-    python tests/golden/make_golden.py [--long]
+    python tests/golden/make_golden.py [--long] [--c2]
 --long also produces the full-length c0 (2000 steps) and c1 (8000 steps)
-recorder series, which take tens of minutes on the host.
+recorder series, which take tens of minutes on the host; --c2 the runs of
+three c2 scenes (300-400 steps, a few minutes).
 """
 from __future__ import annotations
 
@@ -74,7 +75,7 @@ def run_and_store(name, air, src, rec, params, steps, series, fields=True, threa
     return res
 
 
-def main(long_runs=False):
+def main(long_runs=False, c2_runs=False):
     # --- setup fixtures: the reference's own scene files and synthetic ones ---
     for fname, h in (("scene-1.txt", 0.1), ("scene-2.txt", 0.1), ("scene-3.txt", 0.1),
                      ("scene-3.txt", 0.025), ("hall.txt", 0.2)):
@@ -106,6 +107,8 @@ def main(long_runs=False):
     sc = c0["scenes"][0]
     run_and_store("c0_40", sc["air"], sc["sources"], sc["recorders"], params_for(0.05), 40, sc["series"],
                   fields=True, threads=8)
+    if c2_runs:
+        c2_golden_runs()
     if long_runs:
         c0 = K.config("c0")
         sc = c0["scenes"][0]
@@ -117,5 +120,19 @@ def main(long_runs=False):
                       c1["steps"], sc["series"], fields=False, threads=8)
 
 
+# c2 scenes (seeded guillotine decompositions, h = 0.05 m, cell units) run by
+# the reference for a few hundred steps: the batched GPU context is checked
+# against these scene by scene
+C2_RUNS = ((0, 300), (1, 400), (3, 400))
+
+
+def c2_golden_runs():
+    c2 = K.config("c2", steps=max(t for _, t in C2_RUNS))
+    for i, steps in C2_RUNS:
+        sc = c2["scenes"][i]
+        run_and_store(f"c2scene{i}", sc["air"], sc["sources"], sc["recorders"], params_for(0.05), steps,
+                      [s[:steps] for s in sc["series"]], fields=False, threads=1)
+
+
 if __name__ == "__main__":
-    main(long_runs="--long" in sys.argv)
+    main(long_runs="--long" in sys.argv, c2_runs="--c2" in sys.argv)

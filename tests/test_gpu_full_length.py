@@ -1,9 +1,13 @@
 """Full-length benchmark scenes against the reference's own CPU solver.
 
 The reference build ran c0 (2000 steps) and c1 (8000 steps) to produce the
-golden recorder series; the GPU FP32 path must stay within 1e-4 relative L2
-of it, and so must the FP64 GPU oracle.  The FP32-vs-FP64 error is
-reported."""
+golden recorder series.  Two bars, side by side:
+  * reference arithmetic (FP32, the reference's tables and update order)
+    within 1e-4 relative L2 of the reference's CPU solver;
+  * accurate arithmetic (the default) within 1e-4 of the FP64 GPU oracle,
+    and no farther from the reference's CPU solver than that solver's own
+    FP32 rounding puts it from FP64 (+1e-5).
+All cross errors are printed (pytest -s)."""
 import numpy as np
 import pytest
 
@@ -46,3 +50,6 @@ def test_full_length(name):
         print(name, "recorder", r, " ".join(f"{k}={v:.2e}" for k, v in e.items()))
         assert e["ref_vs_reference"] < 1e-4
         assert e["acc_vs_fp64"] < 1e-4
+        # the default (accurate) arithmetic against the reference's CPU solver: no farther than the
+        # reference's own FP32 solution lies from FP64, plus 1e-5
+        assert e["acc_vs_reference"] <= e["fp64_vs_reference"] + 1e-5

@@ -369,3 +369,39 @@ def test_gemm_face_transforms_fp32_match_oracle(path, monkeypatch):
     got = sim.recorders(f64=True)
     for r in range(want.shape[1]):
         assert rel_l2(got[:, r], want[:, r]) < F32_TOL, r
+
+
+@pytest.mark.parametrize("arith", [A.ARITH_ACCURATE, A.ARITH_REFERENCE])
+def test_batched_c2_scenes_match_reference(arith):
+    """Three c2 scenes (seeded guillotine decompositions, h = 0.05 m, 7-11 air
+    partitions each) in ONE batched FP32 context, every scene's recorders
+    within the FP32 bar of the reference's own run of that scene
+    (tests/golden/make_golden.py --c2), in both arithmetic modes."""
+    runs = [(n, load_run(n)) for n in ("c2scene0", "c2scene1", "c2scene3")]
+    runs = [(n, g) for n, g in runs if g is not None]
+    if not runs:
+        pytest.skip("c2 goldens not generated")
+    scenes = []
+    for _, g in runs:
+        sc, p = g["scene"], g["scene"]["params"]
+        scenes.append(A.build_scene(sc["air"], sc["sources"], sc["recorders"], p["dh"], p["dt"], p["c0"],
+                                    p["pml_layers"]))
+    T = max(g["scene"]["steps"] for _, g in runs)
+    sim = A.Simulation(scenes, max_steps=T, arithmetic=arith)
+    for si, (_, g) in enumerate(runs):
+        for i, s in enumerate(g["sources"]):
+            ser = np.zeros(T, np.float32)
+            ser[:len(s)] = s
+            sim.set_source_series(i, ser, scene=si)
+    sim.run(T)
+    checked = 0
+    for si, (name, g) in enumerate(runs):
+        got = sim.recorders(scene=si, f64=True)
+        want = g["recorders"]
+        n = g["scene"]["steps"]
+        for r in range(want.shape[1]):
+            if np.isnan(want[0, r]) or np.abs(want[:, r]).max() == 0:
+                continue
+            assert rel_l2(got[:n, r], want[:, r]) < F32_TOL, (name, r)
+            checked += 1
+    assert checked >= 6
