@@ -443,12 +443,26 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     D.nby = (D.h + D.rpc - 1) / D.rpc;
     col_tiles += (long long)D.nbx * D.nby;
   }
-  // resident slots: 2 tiles per SM; split kz only while the tiles still fit one wave
+  // resident slots: 2 tiles per SM.  kz splits: as many as still fit one
+  // wave, then more while that evens out the last wave (the blocks take the
+  // tiles round-robin, so a last wave that is half full costs a whole tile
+  // time: c4's 749 full-depth columns are 2.46 waves of 304 slots, split in
+  // two they are 4.93)
   const long long slots = (long long)ctx->num_sms * 2 * std::max(1, ctx->tune_tiles);
+  long long nbz_all = col_tiles > 0 ? std::max(1LL, slots / col_tiles) : 1;
+  if (col_tiles > 0) {
+    auto wave_eff = [&](long long nb) {
+      const long long T = col_tiles * nb, waves = (T + slots - 1) / slots;
+      return (double)T / (double)(waves * slots);
+    };
+    const long long base = nbz_all;
+    double best = wave_eff(base);
+    for (long long nb = base + 1; nb <= 4 * base + 4; ++nb)
+      if (wave_eff(nb) > best + 0.03) { best = wave_eff(nb); nbz_all = nb; }
+  }
   for (size_t k = 0; k < ctx->dct.size(); ++k) {
     DctDev& D = ctx->dct[k];
-    long long nbz = col_tiles > 0 ? slots / col_tiles : 1;
-    nbz = std::max(1LL, std::min<long long>(nbz, D.d / 2));
+    long long nbz = std::max(1LL, std::min<long long>(nbz_all, D.d / 2));
     int TZ = (int)((D.d + nbz - 1) / nbz);
     if (TZ < D.d) TZ += TZ & 1;  // even, so every kz tile starts on an even plane
     D.TZ = TZ;
