@@ -437,28 +437,35 @@ static __global__ void __launch_bounds__(kMmaThreads, 1) face_mma_kernel(MmaArgs
     const int m = q * 32 + lane;             // accumulator row = TMEM lane
     uint32_t tc = 0;
     for (int tile = blockIdx.x; tile < a.total && !s_abort; tile += gridDim.x, ++tc) {
+      // the job's fields in registers: the stores below go through a float
+      // pointer into the pool, which the compiler cannot prove leaves the job
+      // table alone, so fields read through J inside the loop would be loaded
+      // again after every store
       const MmaJob& J = a.jobs[mma_find_job(a, sfirst, cached, tile)];
       const int t = tile - J.first;
-      const int mi = t / J.nt, ni = t - mi * J.nt;
-      const int n0 = ni * J.bn;
-      const int g = mi * 128 + m;
-      const bool mok = g < J.nout * J.R;
-      const int o = mok ? g / J.R : 0;
-      const int r = mok ? g - o * J.R : 0;
-      float* outp = buf + J.out[o] + r;
+      const int nt = J.nt, bn = J.bn, R = J.R;
+      const int mi = t / nt, ni = t - mi * nt;
+      const int n0 = ni * bn;
+      const int ncols = min(bn, J.N - n0);          // columns of this tile inside the transform
+      const long long ldo = J.ldo;
       const float scale = J.scale;
+      const int g = mi * 128 + m;
+      const bool mok = g < J.nout * R;
+      const int o = mok ? g / R : 0;
+      const int r = mok ? g - o * R : 0;
+      float* outp = buf + J.out[o] + r + (long long)n0 * ldo;
       const uint32_t acc = tc & 1;
       if (!mbar_wait_bounded(&accfull[acc], (tc >> 1) & 1, &s_abort)) break;
       tc_fence_after();
-      for (int cg = 0; cg * 32 < J.bn; ++cg) {
+      for (int cg = 0; cg * 32 < bn; ++cg) {
         float v[32];
         tmem_ld32(tmem + acc * kMmaAccCols + ((uint32_t)(q * 32) << 16) + (uint32_t)(cg * 32), v);
         if (mok) {
+          float* op = outp + (long long)(cg * 32) * ldo;
+          const int lim = ncols - cg * 32;
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            const int n = n0 + cg * 32 + i;
-            if (cg * 32 + i < J.bn && n < J.N) outp[(long long)n * J.ldo] = v[i] * scale;
-          }
+          for (int i = 0; i < 32; ++i)
+            if (i < lim) op[(long long)i * ldo] = v[i] * scale;
         }
       }
       tc_fence_before();
