@@ -55,7 +55,7 @@ __device__ __forceinline__ T adj_force(const IfaceAdjArgs<T>& a, int type, const
     return o >= 0 ? a.buf[o - D.fX + D.aX] : (T)0;
   }
   const PmlDev& P = a.pml[s.idx];
-  return a.dt * a.dt * a.buf[P.ap[a.lin] + ((long long)c * P.A + v) * P.B + u];
+  return a.dt * a.dt * a.buf[P.ap[a.lin] + ((long long)c * P.A + v) * P.Bp + u];
 }
 
 template <typename T>
@@ -73,7 +73,7 @@ __device__ __forceinline__ void adj_pressure_add(const IfaceAdjArgs<T>& a, int t
     return;
   }
   const PmlDev& P = a.pml[s.idx];
-  atomicAdd(a.buf + P.ap[a.lout] + ((long long)c * P.A + v) * P.B + u, val);
+  atomicAdd(a.buf + P.ap[a.lout] + ((long long)c * P.A + v) * P.Bp + u, val);
 }
 
 // Transpose of iface_kernel: every force value the forward step writes
@@ -181,12 +181,12 @@ __global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
   for (int bi = blockIdx.x; bi < a.nblocks; bi += gridDim.x) {
     const int4 blk = a.blocks[bi];
     const PmlDev& P = a.pml[blk.x];
-    const int L = P.L, A = P.A, B = P.B;
+    const int L = P.L, A = P.A, B = P.B, Bp = P.Bp;
     const int a0 = blk.y, b0 = blk.z;
     const int ia = a0 + ta, ib = b0 + tb;
     const bool inside = ia < A && ib < B;
-    const long long lstride = (long long)A * B;
-    const long long col = inside ? (long long)ia * B + ib : 0;
+    const long long lstride = (long long)A * Bp;
+    const long long col = inside ? (long long)ia * Bp + ib : 0;
     const T* X = a.buf + P.ap[a.lx];
     T* Y = a.buf + P.ap[a.ly];
     T* O = a.buf + P.ap[a.lo];
@@ -227,21 +227,21 @@ __global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
         const int i = threadIdx.x + 256 * k;
         const int r = i / (TB + 6), c = i - r * (TB + 6);
         const int aa = a0 + r - 3, bb = b0 + c - 3;
-        nX[k] = (i < (TA + 6) * (TB + 6) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? Xl[(long long)aa * B + bb] : (T)0;
+        nX[k] = (i < (TA + 6) * (TB + 6) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? Xl[(long long)aa * Bp + bb] : (T)0;
       }
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         const int i = threadIdx.x + 256 * k;
         const int r = i / TB, c = i - r * TB;
         const int aa = a0 + r - 2, bb = b0 + c;
-        nA[k] = (i < (TA + 4) * TB && aa >= 0 && aa < A && bb < B) ? fal[(long long)aa * B + bb] : (T)0;
+        nA[k] = (i < (TA + 4) * TB && aa >= 0 && aa < A && bb < B) ? fal[(long long)aa * Bp + bb] : (T)0;
       }
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         const int i = threadIdx.x + 256 * k;
         const int r = i / (TB + 4), c = i - r * (TB + 4);
         const int aa = a0 + r, bb = b0 + c - 2;
-        nB[k] = (i < TA * (TB + 4) && aa < A && bb >= 0 && bb < B) ? fbl[(long long)aa * B + bb] : (T)0;
+        nB[k] = (i < TA * (TB + 4) && aa < A && bb >= 0 && bb < B) ? fbl[(long long)aa * Bp + bb] : (T)0;
       }
       const long long I = l * lstride + col;
       ny = inside ? Y[I] : (T)0;
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
           const int i = threadIdx.x + 256 * k;
           const int r = i / (TB + 4), c = i - r * (TB + 4);
           const int aa = a0 + r - 2, bb = b0 + c - 2;
-          nQ[k] = (i < (TA + 4) * (TB + 4) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? hpl[(long long)aa * B + bb]
+          nQ[k] = (i < (TA + 4) * (TB + 4) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? hpl[(long long)aa * Bp + bb]
                                                                                         : (T)0;
         }
         npp = inside ? hpp[I] : (T)0;

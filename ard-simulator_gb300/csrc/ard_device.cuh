@@ -78,16 +78,18 @@ struct PointDev {
 struct PmlDev {
   int type;               // ARD_PML_*
   int L, A, B;            // layers along the normal; plane A x B (B fastest)
+  int Bp;                 // row pitch of the plane: B rounded up to 4 (rows start on 16-byte
+                          // boundaries, as the tensor-map tile loads of the PML kernel need)
   int strip0;             // first layer of the forced strip (L-3 or 0)
   int scene;
   long long p[2];
   long long phn[2], pha[2], phb[2];
-  long long force;        // [3][A][B]
+  long long force;        // [3][A][Bp]
   long long ap[3];         // adjoint of p (three rotating levels)
   long long aphn[2], apha[2], aphb[2];
-  long long aforce;        // adjoint of the strip force [3][A][B]
+  long long aforce;        // adjoint of the strip force [3][A][Bp]
   long long zeta;         // [L] damping profile (scaled)
-  long long n;            // L*A*B
+  long long n;            // L*A*Bp elements (padding columns stay zero)
   long long hoff;         // offset of the slab inside each all-slab region (p, phi: same for all eight)
   long long foff;         // offset of the slab's strip force inside the all-slab strip region
 };

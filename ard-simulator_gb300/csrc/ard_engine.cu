@@ -436,7 +436,8 @@ template <typename T>
 int launch_pml(Ctx* ctx, int par, int tstep, cudaStream_t s) {
   if (ctx->pml_blocks.empty()) return ARD_OK;
   PmlArgs<T> pa{reinterpret_cast<T*>(ctx->d_buf), ctx->d_pml, ctx->d_pml_blocks, (int)ctx->pml_blocks.size(), par,
-                (T)ctx->dt, (T)ctx->dh, (T)ctx->c0, (const PmlHist<T>*)ctx->d_phist, ctx->d_t, tstep};
+                (T)ctx->dt, (T)ctx->dh, (T)ctx->c0, (const PmlHist<T>*)ctx->d_phist, ctx->d_t, tstep,
+                ctx->d_pml_maps, ctx->d_err};
   ARD_CUDA(launch_dep(pml_kernel<T>, grid_for((long long)ctx->pml_blocks.size(), 1, ctx->num_sms * 8), 256, 0, s, pa));
   ARD_CUDA(cudaGetLastError());
   return ARD_OK;

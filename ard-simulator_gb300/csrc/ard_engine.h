@@ -147,6 +147,7 @@ struct Ctx {
   void* d_phist = nullptr;        // PmlHist<T> read by the PML kernel (adjoint contexts only)
   MmaJob* d_mjobs[4] = {nullptr, nullptr, nullptr, nullptr};
   int* d_err = nullptr;           // set by a kernel whose bounded wait ran out (checked on synchronize)
+  CUtensorMap* d_pml_maps = nullptr;   // tensor maps of the PML tile loads (build_pml_maps)
 
   // neighbourhood recording (ard_record_neighbourhoods): the 10 x 10 x 10
   // pressure cube around every recorder after every step, [max_steps][n_rec_total][1000]
@@ -167,6 +168,7 @@ enum { kStagePml = 0, kStageFwdRows, kStageFwdCols, kStageModal, kStageRecorder,
        kStageIface, kNumStages };
 
 int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes);
+int build_pml_maps(Ctx* ctx);
 void free_ctx_device(Ctx* ctx);
 template <typename T>
 int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, bool fork, cudaEvent_t* ev);

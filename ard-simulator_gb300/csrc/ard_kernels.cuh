@@ -30,6 +30,7 @@
 #include <type_traits>
 #include <utility>
 
+#include "ard_async.cuh"
 #include "ard_device.cuh"
 
 namespace ard {
@@ -1243,22 +1244,48 @@ struct PmlArgs {
   const PmlHist<T>* hist;   // null without the adjoint
   const long long* tcount;
   int tstep;
+  const CUtensorMap* maps;  // per slab: p[0], p[1], pha[0], pha[1], phb[0], phb[1] as [L][A][B] tensors
+  int* err;                 // set to 1 when a bounded wait runs out
+};
+
+// Plane tiles of the PML kernel and the boxes the TMA unit loads per layer:
+// p with a halo of 3 along a and of 4 / 4 along b (x starts at b0 - 4, on a
+// 16-byte boundary), phi_a with a halo of 2 along a, phi_b with a halo of 4 /
+// 4 along b; each box 128-byte aligned in the stage.
+constexpr int kPmlTA = 8, kPmlTB = 32;
+template <typename T>
+struct PmlStage {
+  static constexpr int PW = kPmlTB + 8;                                  // p and phi_b box width
+  static constexpr int ps = (kPmlTA + 6) * PW * (int)sizeof(T);
+  static constexpr int psa = (ps + 127) & ~127;
+  static constexpr int fa = (kPmlTA + 4) * kPmlTB * (int)sizeof(T);
+  static constexpr int fb = kPmlTA * PW * (int)sizeof(T);
+  static constexpr int fba = (fb + 127) & ~127;
+  static constexpr int bytes = psa + fa + fba;
+  static constexpr int tx = ps + fa + fb;                                 // bytes the three boxes deliver
 };
 
 // Grote-Sim PML (pml_partition.cpp:113-200) in slab coordinates: layer l
 // along the normal, (a, b) in the plane; outside the slab every field reads
 // zero (the reference's sentinel cell).  Only the normal damping zeta_n is
 // non-zero in a slab (zeta_a = zeta_b = 0 in the reference's formulas).
-// A block owns an 8 x 32 plane tile and walks the layers: the tile of p (halo
-// 3) and of phi_a / phi_b (halo 2 along their own axis) is staged in shared
-// memory per layer; the normal-axis stencils run from a register window.
+// A block owns an 8 x 32 plane tile and walks the layers.  The in-plane
+// stencils read tiles of p(t-1) (halo 3), phi_a and phi_b (halo 2 along
+// their own axis) that the TMA unit brings into a two-stage ring of shared
+// memory, one layer ahead, across the block's tiles; the tensor maps'
+// zero fill outside the slab is the sentinel.  The normal-axis stencils run
+// from register windows; p(t-2) and the strip force of the next layer are
+// fetched into registers while the current one computes.  Every wait is
+// bounded: one that runs out sets the kernel's error word and the block
+// leaves its loops.
 template <typename T>
 __global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
   grid_dependency_wait();
-  constexpr int TA = 8, TB = 32;
-  __shared__ T Ps[TA + 6][TB + 6];
-  __shared__ T FA[TA + 4][TB];
-  __shared__ T FB[TA][TB + 4];
+  using S = PmlStage<T>;
+  constexpr int TA = kPmlTA, TB = kPmlTB, PW = S::PW;
+  __shared__ __align__(128) unsigned char stage[2][S::bytes];
+  __shared__ uint64_t bar[2];
+  __shared__ volatile int s_abort;
   const T c7[7] = {2, -27, 270, -490, 270, -27, 2};
   const T c5[5] = {1, -8, 0, 8, -1};
   const int tb = threadIdx.x & 31, ta = threadIdx.x >> 5;
@@ -1276,20 +1303,55 @@ __global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
     if (h.f && t >= h.ft0 && t < h.ft1) hf = h.f + (t - h.ft0) * h.flen;
     if (h.fsrc) fsrc = h.fsrc + (t - h.fs0) * h.flen;
   }
-  for (int bi = blockIdx.x; bi < a.nblocks; bi += gridDim.x) {
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init_fence();
+    s_abort = 0;
+  }
+  __syncthreads();
+  // thread 0's issue cursor: the block's (tile, layer) sequence, one layer
+  // ahead of the computation (two stages)
+  int ibi = blockIdx.x, il = 0, iL = 0;
+  uint32_t issued = 0;
+  const int lev = a.par ^ 1;   // time level t-1 of p, phi_a, phi_b
+  auto issue_next = [&]() {
+    if (ibi >= a.nblocks) return;
+    const int4 blk = a.blocks[ibi];
+    if (il == 0) iL = a.pml[blk.x].L;
+    const CUtensorMap* mp = a.maps + 6LL * blk.x;
+    const int sg = (int)(issued & 1);
+    unsigned char* sb = stage[sg];
+    mbar_arrive_expect_tx(&bar[sg], (uint32_t)S::tx);
+    tma_load_3d(sb, mp + lev, blk.z - 4, blk.y - 3, il, &bar[sg]);
+    tma_load_3d(sb + S::psa, mp + 2 + lev, blk.z, blk.y - 2, il, &bar[sg]);
+    tma_load_3d(sb + S::psa + S::fa, mp + 4 + lev, blk.z - 4, blk.y, il, &bar[sg]);
+    ++issued;
+    if (++il == iL) {
+      il = 0;
+      ibi += gridDim.x;
+    }
+  };
+  if (threadIdx.x == 0) {
+    issue_next();
+    issue_next();
+  }
+  uint32_t used = 0;   // layers consumed by the block (uniform)
+  bool stop = false;
+  for (int bi = blockIdx.x; bi < a.nblocks && !stop; bi += gridDim.x) {
     const int4 blk = a.blocks[bi];
     const PmlDev& P = a.pml[blk.x];
-    const int L = P.L, A = P.A, B = P.B;
+    const int L = P.L, A = P.A, B = P.B, Bp = P.Bp;
+    const int strip0 = P.strip0;       // held in registers: the layer loop stores through the pool pointer
+    const long long hoff = P.hoff;
     const int a0 = blk.y, b0 = blk.z;
     const int ia = a0 + ta, ib = b0 + tb;
     const bool inside = ia < A && ib < B;
-    const long long lstride = (long long)A * B;
-    const long long col = inside ? (long long)ia * B + ib : 0;
+    const long long lstride = (long long)A * Bp;
+    const long long col = inside ? (long long)ia * Bp + ib : 0;
     const T* p = a.buf + P.p[a.par ^ 1];   // p(t-1)
     T* pn = a.buf + P.p[a.par];            // p(t-2) -> p(t)
     const T* fn = a.buf + P.phn[a.par ^ 1];
-    const T* fa = a.buf + P.pha[a.par ^ 1];
-    const T* fb = a.buf + P.phb[a.par ^ 1];
     T* fn_o = a.buf + P.phn[a.par];
     T* fa_o = a.buf + P.pha[a.par];
     T* fb_o = a.buf + P.phb[a.par];
@@ -1309,93 +1371,42 @@ __global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
       fw[m] = (inside && ll >= 0 && ll < L) ? fn[ll * lstride + col] : (T)0;
     }
     const T r180 = (T)1 / ((T)180 * a.dh * a.dh), r12 = (T)1 / ((T)12 * a.dh), rdt = (T)1 / a.dt;
-    // tiles of the next layer are fetched into registers while the current
-    // layer computes (3 + 2 + 2 values per thread, plus p(t-2) and the force);
-    // the in-layer offsets of a thread's tile elements (-1: outside the slab
-    // or the tile, read as zero) are the same for every layer
-    int oP[3], oA[2], oB[2];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const int i = threadIdx.x + 256 * k;
-      const int r = i / (TB + 6), c = i - r * (TB + 6);
-      const int aa = a0 + r - 3, bb = b0 + c - 3;
-      oP[k] = (i < (TA + 6) * (TB + 6) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? aa * B + bb : -1;
-    }
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const int i = threadIdx.x + 256 * k;
-      const int r = i / TB, c = i - r * TB;
-      const int aa = a0 + r - 2, bb = b0 + c;
-      oA[k] = (i < (TA + 4) * TB && aa >= 0 && aa < A && bb < B) ? aa * B + bb : -1;
-    }
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const int i = threadIdx.x + 256 * k;
-      const int r = i / (TB + 4), c = i - r * (TB + 4);
-      const int aa = a0 + r, bb = b0 + c - 2;
-      oB[k] = (i < TA * (TB + 4) && aa < A && bb >= 0 && bb < B) ? aa * B + bb : -1;
-    }
-    T nP[3], nA[2], nB[2], nold = 0, nforce = 0;
+    T nold = 0, nforce = 0;
     auto fetch = [&](int l) {
-      const T* pl = p + l * lstride;
-      const T* fal = fa + l * lstride;
-      const T* fbl = fb + l * lstride;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) nP[k] = oP[k] >= 0 ? pl[oP[k]] : (T)0;
-#pragma unroll
-      for (int k = 0; k < 2; ++k) nA[k] = oA[k] >= 0 ? fal[oA[k]] : (T)0;
-#pragma unroll
-      for (int k = 0; k < 2; ++k) nB[k] = oB[k] >= 0 ? fbl[oB[k]] : (T)0;
-      const int sl = l - P.strip0;
+      const int sl = l - strip0;
       nold = inside ? pn[l * lstride + col] : (T)0;
       nforce = (inside && sl >= 0 && sl < 3) ? force[sl * lstride + col] : (T)0;
     };
-    // the tiles as flat arrays: element i of a thread's k-th value
-    auto commit = [&]() {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const int i = threadIdx.x + 256 * k;
-        if (i < (TA + 6) * (TB + 6)) (&Ps[0][0])[i] = nP[k];
-      }
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int i = threadIdx.x + 256 * k;
-        if (i < (TA + 4) * TB) (&FA[0][0])[i] = nA[k];
-      }
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int i = threadIdx.x + 256 * k;
-        if (i < TA * (TB + 4)) (&FB[0][0])[i] = nB[k];
-      }
-    };
     fetch(0);
     for (int l = 0; l < L; ++l) {
-      __syncthreads();  // previous layer done with the tiles
-      commit();
+      const int sg = (int)(used & 1);
+      mbar_wait_bounded(&bar[sg], (used >> 1) & 1, &s_abort);
+      const T* Ps = reinterpret_cast<const T*>(stage[sg]);                    // [TA + 6][PW], b from b0 - 4
+      const T* FA = reinterpret_cast<const T*>(stage[sg] + S::psa);           // [TA + 4][TB], b from b0
+      const T* FB = reinterpret_cast<const T*>(stage[sg] + S::psa + S::fa);   // [TA][PW], b from b0 - 4
       const T pold = nold, f = nforce;
       if (l + 1 < L) fetch(l + 1);
-      __syncthreads();
       if (force_rec && inside) {
-        const int sl = l - P.strip0;
+        const int sl = l - strip0;
         if (sl >= 0 && sl < 3) force_rec[sl * lstride + col] = f;
       }
-      if (inside) {
+      if (inside && !s_abort) {
         T ln = 0, la = 0, lb = 0;
 #pragma unroll
         for (int m = 0; m < 7; ++m) {
           ln += c7[m] * pw[m];
-          la += c7[m] * Ps[ta + m][tb + 3];
-          lb += c7[m] * Ps[ta + 3][tb + m];
+          la += c7[m] * Ps[(ta + m) * PW + tb + 4];
+          lb += c7[m] * Ps[(ta + 3) * PW + tb + 1 + m];
         }
         T un = 0, ua = 0, ub = 0, gn = 0, ga = 0, gb = 0;
 #pragma unroll
         for (int m = 0; m < 5; ++m) {
           un += c5[m] * pw[m + 1];
-          ua += c5[m] * Ps[ta + 1 + m][tb + 3];
-          ub += c5[m] * Ps[ta + 3][tb + 1 + m];
+          ua += c5[m] * Ps[(ta + 1 + m) * PW + tb + 4];
+          ub += c5[m] * Ps[(ta + 3) * PW + tb + 2 + m];
           gn += c5[m] * fw[m];
-          ga += c5[m] * FA[ta + m][tb];
-          gb += c5[m] * FB[ta][tb + m];
+          ga += c5[m] * FA[(ta + m) * TB + tb];
+          gb += c5[m] * FB[ta * PW + tb + 2 + m];
         }
         ln *= r180; la *= r180; lb *= r180;
         un *= r12; ua *= r12; ub *= r12;
@@ -1411,11 +1422,11 @@ __global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
         const T fnew = fnc - a.dt * zn * fnc + a.dt * (-zn) * un;
         fn_o[I] = fnew;
         if (hp) {
-          hp[P.hoff + I] = pnew;
-          hfn[P.hoff + I] = fnew;
+          hp[hoff + I] = pnew;
+          hfn[hoff + I] = fnew;
         }
-        fa_o[I] = FA[ta + 2][tb] + a.dt * zn * ua;
-        fb_o[I] = FB[ta][tb + 2] + a.dt * zn * ub;
+        fa_o[I] = FA[(ta + 2) * TB + tb] + a.dt * zn * ua;
+        fb_o[I] = FB[ta * PW + tb + 4] + a.dt * zn * ub;
       }
       // slide the windows one layer
 #pragma unroll
@@ -1424,7 +1435,25 @@ __global__ void __launch_bounds__(256, 4) pml_kernel(PmlArgs<T> a) {
 #pragma unroll
       for (int m = 0; m < 4; ++m) fw[m] = fw[m + 1];
       fw[4] = (inside && l + 3 < L) ? fn[(l + 3) * lstride + col] : (T)0;
+      __syncthreads();   // every thread is done with stage sg
+      if (s_abort) {
+        stop = true;
+        break;
+      }
+      if (threadIdx.x == 0) issue_next();
+      ++used;
     }
+  }
+  if (s_abort) {
+    // a wait ran out: report it, and give loads still in flight time to land
+    // (bounded) before the block's shared memory is released
+    if (threadIdx.x == 0) {
+      atomicExch(a.err, 1);
+      const long long t0 = clock64();
+      while (clock64() - t0 < 20000000LL) {
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -1486,25 +1515,35 @@ __global__ void __launch_bounds__(256) iface_kernel(IfaceArgs<T> a) {
       ph[n] = a.buf[I.hi.pb[n][a.par] + (long long)hv * I.hi.psv + hu];
     }
     const T absorp = (T)I.absorption;
+    // every offset and value first, the six stores after them: a store
+    // through the pool pointer may alias the descriptor table as far as the
+    // compiler can tell, so descriptor fields read after a store are loaded
+    // again
+    long long o[6];
+    T val[6];
 #pragma unroll
     for (int m = -3; m < 3; ++m) {
+      o[m + 3] = -1;
+      val[m + 3] = 0;
       if (!(mask & (1u << (m + 3)))) continue;
       T sip1 = 0, sip2 = 0;
 #pragma unroll
       for (int n = 0; n < 3; ++n) sip1 += C[m + 3][n] * pl[n];
 #pragma unroll
       for (int n = 3; n < 6; ++n) sip2 += C[m + 3][n] * ph[n - 3];
-      long long o;
       T sip;
       if (m < 0) {
         sip = I.lo.self ? (sip1 + sip2) : sip2;
-        o = side_force_offset(I.lo, I.type, I.lo.ext + m, lu, lv);
+        o[m + 3] = side_force_offset(I.lo, I.type, I.lo.ext + m, lu, lv);
       } else {
         sip = I.hi.self ? (sip1 + sip2) : sip1;
-        o = side_force_offset(I.hi, I.type, m, hu, hv);
+        o[m + 3] = side_force_offset(I.hi, I.type, m, hu, hv);
       }
-      if (o >= 0) a.buf[o] = absorp * (sip * k0);
+      val[m + 3] = absorp * (sip * k0);
     }
+#pragma unroll
+    for (int m = 0; m < 6; ++m)
+      if (o[m] >= 0) a.buf[o[m]] = val[m];
   }
 }
 

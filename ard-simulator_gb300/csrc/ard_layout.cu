@@ -1,6 +1,8 @@
 // Context layout: turns flattened scenes (the reference's partitions,
 // boundaries, sources and recorders) into device work tables and an HBM
 // element pool; plus the setup and readout entry points of the C ABI.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -366,7 +368,8 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         if (ax == ARD_BOUNDARY_X) { P.L = p.width; P.A = p.depth; P.B = p.height; }
         else if (ax == ARD_BOUNDARY_Y) { P.L = p.height; P.A = p.depth; P.B = p.width; }
         else { P.L = p.depth; P.A = p.height; P.B = p.width; }
-        P.n = (long long)P.L * P.A * P.B;
+        P.Bp = (P.B + 3) & ~3;
+        P.n = (long long)P.L * P.A * P.Bp;
         P.strip0 = -1;
         rec.engine_idx[i] = (int)ctx->pml.size();
         ctx->pml.push_back(P);
@@ -494,7 +497,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   }
   ctx->force_begin = pool.off;
   for (PmlDev& P : ctx->pml) {
-    P.force = pool.take(3LL * P.A * P.B);
+    P.force = pool.take(3LL * P.A * P.Bp);
     P.foff = P.force - ctx->force_begin;
   }
   ctx->state_end = pool.off;
@@ -516,7 +519,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     for (PmlDev& P : ctx->pml) {
       for (int k = 0; k < 3; ++k) P.ap[k] = pool.take(P.n);
       for (int k = 0; k < 2; ++k) { P.aphn[k] = pool.take(P.n); P.apha[k] = pool.take(P.n); P.aphb[k] = pool.take(P.n); }
-      P.aforce = pool.take(3LL * P.A * P.B);
+      P.aforce = pool.take(3LL * P.A * P.Bp);
     }
     ctx->adj_end = pool.off;
   }
@@ -555,7 +558,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
       return ARD_ERR_INVALID;
     }
     P.zeta = pool.take(P.L);
-    ctx->n_pml_cells += P.n;
+    ctx->n_pml_cells += (long long)P.L * P.A * P.B;
     for (int a0 = 0; a0 < P.A; a0 += 8)
       for (int b0 = 0; b0 < P.B; b0 += 32) ctx->pml_blocks.push_back(make_int4((int)k, a0, b0, 0));
   }
@@ -703,9 +706,9 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
           S.pb[n][0] = S.pb[n][1] = b;
         } else {
           const PmlDev& P = ctx->pml[S.idx];
-          S.pb[n][0] = P.p[0] + (long long)c * P.A * P.B;
-          S.pb[n][1] = P.p[1] + (long long)c * P.A * P.B;
-          S.psv = P.B;
+          S.pb[n][0] = P.p[0] + (long long)c * P.A * P.Bp;
+          S.pb[n][1] = P.p[1] + (long long)c * P.A * P.Bp;
+          S.psv = P.Bp;
         }
       }
       if (S.kind == 0) {
@@ -714,9 +717,9 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
         S.w = D.w; S.h = D.h; S.d = D.d; S.wp = D.wp;
       } else {
         const PmlDev& P = ctx->pml[S.idx];
-        S.fls = (long long)P.A * P.B;
+        S.fls = (long long)P.A * P.Bp;
         S.fb = P.force - (long long)P.strip0 * S.fls;
-        S.fsv = P.B;
+        S.fsv = P.Bp;
       }
     }
     for (long long k = 0; k < (long long)(I.u1 - I.u0) * (I.v1 - I.v0); ++k) ctx->cell_iface.push_back((int)ctx->ifs.size());
@@ -966,6 +969,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     if (ctx->mma_faces && (rc = up(&ctx->d_mjobs[k], ctx->mjobs[k]))) return rc;
   ARD_CUDA(cudaMalloc(&ctx->d_err, sizeof(int)));
   ARD_CUDA(cudaMemset(ctx->d_err, 0, sizeof(int)));
+  if (int rc = build_pml_maps(ctx)) return rc;
   if (ctx->adjoint) {
     if ((rc = up(&ctx->d_adj1_2d, ctx->adj1_2d))) return rc;
     if ((rc = up(&ctx->d_adj2_2d, ctx->adj2_2d))) return rc;
@@ -1032,7 +1036,7 @@ void free_ctx_device(Ctx* ctx) {
                   ctx->d_hist, ctx->d_t, ctx->d_adj1_2d, ctx->d_adj2_2d, ctx->d_adjg[0], ctx->d_adjg[1],
                   ctx->d_adjg[2], ctx->d_adjg[3], ctx->d_tb, ctx->d_phist, ctx->d_psum,
                   ctx->d_cell_iface, ctx->d_mjobs[0], ctx->d_mjobs[1], ctx->d_mjobs[2], ctx->d_mjobs[3],
-                  ctx->d_err};
+                  ctx->d_err, ctx->d_pml_maps};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
@@ -1044,6 +1048,56 @@ void free_ctx_device(Ctx* ctx) {
   ctx->graph_exec = nullptr;
   ctx->d_buf = nullptr;
   ctx->d_buf_base = nullptr;
+}
+
+// cuTensorMapEncodeTiled, reached through the runtime's driver entry point
+// (the library links only the CUDA runtime).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// The tensor maps of the PML kernel's tile loads: per slab p, phi_a and phi_b
+// of both time levels as [L][A][B] tensors (row pitch Bp), with the box of
+// the tile each one feeds (PmlStage).  Elements outside the tensor read as
+// zero, the reference's sentinel.
+int build_pml_maps(Ctx* ctx) {
+  if (ctx->pml.empty()) return ARD_OK;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) { ctx->err = "cuTensorMapEncodeTiled is not available from the driver"; return ARD_ERR_CUDA; }
+  const size_t es = elem_size(ctx);
+  const CUtensorMapDataType type =
+      ctx->prec == ARD_PREC_F64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  const cuuint32_t boxes[3][3] = {{(cuuint32_t)kPmlTB + 8, (cuuint32_t)kPmlTA + 6, 1},   // p: halo 3 (b from b0 - 4)
+                                  {(cuuint32_t)kPmlTB, (cuuint32_t)kPmlTA + 4, 1},       // phi_a: halo 2 along a
+                                  {(cuuint32_t)kPmlTB + 8, (cuuint32_t)kPmlTA, 1}};      // phi_b: halo 2 along b
+  const cuuint32_t estr[3] = {1, 1, 1};
+  std::vector<CUtensorMap> maps(6 * ctx->pml.size());
+  for (size_t k = 0; k < ctx->pml.size(); ++k) {
+    const PmlDev& P = ctx->pml[k];
+    const cuuint64_t dims[3] = {(cuuint64_t)P.B, (cuuint64_t)P.A, (cuuint64_t)P.L};
+    const cuuint64_t strides[2] = {(cuuint64_t)P.Bp * es, (cuuint64_t)P.A * P.Bp * es};
+    const long long offs[6] = {P.p[0], P.p[1], P.pha[0], P.pha[1], P.phb[0], P.phb[1]};
+    for (int q = 0; q < 6; ++q) {
+      const CUresult r = enc(&maps[6 * k + q], type, 3, (char*)ctx->d_buf + offs[q] * es, dims, strides, boxes[q / 2],
+                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) {
+        ctx->err = "cuTensorMapEncodeTiled failed for a PML slab (error " + std::to_string((int)r) + ")";
+        return ARD_ERR_CUDA;
+      }
+    }
+  }
+  ARD_CUDA(cudaMalloc(&ctx->d_pml_maps, sizeof(CUtensorMap) * maps.size()));
+  ARD_CUDA(cudaMemcpy(ctx->d_pml_maps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
+  return ARD_OK;
 }
 
 // Dense 3D transform of one air partition, unpadded [d][h][w], from pool
@@ -1314,9 +1368,9 @@ extern "C" int ard_read_field(ard_ctx* c, int32_t scene, int32_t partition, floa
     for (int y = 0; y < p.height; ++y)
       for (int x = 0; x < p.width; ++x) {
         long long s;
-        if (ax == 0) s = ((long long)x * P.A + z) * P.B + y;
-        else if (ax == 1) s = ((long long)y * P.A + z) * P.B + x;
-        else s = ((long long)z * P.A + y) * P.B + x;
+        if (ax == 0) s = ((long long)x * P.A + z) * P.Bp + y;
+        else if (ax == 1) s = ((long long)y * P.A + z) * P.Bp + x;
+        else s = ((long long)z * P.A + y) * P.Bp + x;
         out[((long long)z * p.height + y) * p.width + x] = (float)h[s];
       }
   return ARD_OK;
@@ -1330,7 +1384,7 @@ int check_device_error(Ctx* ctx) {
   int v = 0;
   ARD_CUDA(cudaMemcpy(&v, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (v) {
-    ctx->err = "a tensor-core face transform gave up waiting for its MMAs (device error word set)";
+    ctx->err = "a kernel gave up waiting at one of its barriers (device error word set)";
     return ARD_ERR_CUDA;
   }
   return ARD_OK;

@@ -187,7 +187,7 @@ struct SliceArgs {
   int valid;             // the slice's local coordinate lies inside the partition
   long long plane;       // DCT: pool offset of the slice plane
   long long slab;        // PML: pool offset of p (current level)
-  int ptype, A, B;       // PML slab geometry
+  int ptype, A, B;       // PML slab geometry (B: row pitch)
   int look_from, coord;  // view and the local coordinate passed by the reference
   int ni, nj;            // rows / columns of the partition's slice
   int off_i, off_j;      // its offset in the image
@@ -545,7 +545,7 @@ static int render_slice(Ctx* ctx, int scene, int look_from, int coord, float v_c
       s.slab = Q.p[lvl];
       s.ptype = Q.type;
       s.A = Q.A;
-      s.B = Q.B;   // out of range: PmlPartition::GetIndex's zero sentinel
+      s.B = Q.Bp;   // row pitch; out of range: PmlPartition::GetIndex's zero sentinel
     }
     ARD_CUDA(cudaGetLastError());
     paint_kernel<T><<<blocks, 256, 0, ctx->stream>>>(buf, s, pix, pres);
