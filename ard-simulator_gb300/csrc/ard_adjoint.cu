@@ -105,6 +105,9 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
     if (ctx->fused_faces) {
       ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for((long long)ctx->adj1_2d.size(), 1, gx), kFace2DThreads,
                           ctx->f2d_bytes, s, buf, ctx->d_adj1_2d, (int)ctx->adj1_2d.size(), ctx->f2d_smem));
+    } else if (ctx->mma_faces) {
+      ARD_CUDA(launch_mma(ctx, 4, s));
+      ARD_CUDA(launch_mma(ctx, 5, s));
     } else {
       for (int k = 0; k < 2; ++k)
         ARD_CUDA(launch_face_gemm<T>(buf, ctx->adjg[k].jobs[0], ctx->d_adjg[k], (int)ctx->adjg[k].jobs.size(),
@@ -130,6 +133,9 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
     if (ctx->fused_faces) {
       ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for((long long)ctx->adj2_2d.size(), 1, gx), kFace2DThreads,
                           ctx->f2d_bytes, s, buf, ctx->d_adj2_2d, (int)ctx->adj2_2d.size(), ctx->f2d_smem));
+    } else if (ctx->mma_faces) {
+      ARD_CUDA(launch_mma(ctx, 6, s));
+      ARD_CUDA(launch_mma(ctx, 7, s));
     } else {
       for (int k = 2; k < 4; ++k)
         ARD_CUDA(launch_face_gemm<T>(buf, ctx->adjg[k].jobs[0], ctx->d_adjg[k], (int)ctx->adjg[k].jobs.size(),

@@ -34,14 +34,18 @@ int grid_for(long long work, int per_block, int max_blocks) {
   return (int)b;
 }
 
+}  // namespace
+
+namespace ard {
 // One tensor-core face pass (job list k) on stream s: one CTA per SM at most.
+// (The adjoint's passes launch through here too, so that one instance of the
+// kernel, configured in ard_create, serves both.)
 cudaError_t launch_mma(Ctx* ctx, int k, cudaStream_t s) {
   if (ctx->mtiles[k] == 0) return cudaSuccess;
   MmaArgs a{reinterpret_cast<float*>(ctx->d_buf), ctx->d_mjobs[k], (int)ctx->mjobs[k].size(), ctx->mtiles[k], ctx->d_err};
   return launch_dep(face_mma_kernel, grid_for(ctx->mtiles[k], 1, ctx->num_sms), kMmaThreads, kMmaSmemBytes, s, a);
 }
-
-}  // namespace
+}  // namespace ard
 
 // ---------------------------------------------------------------------------
 // context construction

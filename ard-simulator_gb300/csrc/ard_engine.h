@@ -91,8 +91,8 @@ struct Ctx {
   // form): the four passes as batched split-TF32 products (ard_mma.cuh), with
   // the split transform tables of every extent in the pool.
   bool mma_faces = false;
-  std::vector<MmaJob> mjobs[4];            // forward pass 1, 2; inverse pass 1, 2
-  int mtiles[4] = {0, 0, 0, 0};
+  std::vector<MmaJob> mjobs[8];            // forward pass 1, 2; inverse pass 1, 2; adjoint passes 1 .. 4
+  int mtiles[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   std::vector<std::pair<int, long long>> mma_tables;   // extent -> offset of Chi, Clo, CiThi, CiTlo
   Face2DSmem f2d_smem{0, 0, 0, 0};
   size_t f2d_bytes = 0;
@@ -145,7 +145,7 @@ struct Ctx {
   XformJob* d_adjg[4] = {nullptr, nullptr, nullptr, nullptr};
   long long* d_tb = nullptr;      // adjoint counters {current step, first step of the PML history}
   void* d_phist = nullptr;        // PmlHist<T> read by the PML kernel (adjoint contexts only)
-  MmaJob* d_mjobs[4] = {nullptr, nullptr, nullptr, nullptr};
+  MmaJob* d_mjobs[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   int* d_err = nullptr;           // set by a kernel whose bounded wait ran out (checked on synchronize)
   CUtensorMap* d_pml_maps = nullptr;   // tensor maps of the PML tile loads (build_pml_maps)
 
@@ -169,6 +169,7 @@ enum { kStagePml = 0, kStageFwdRows, kStageFwdCols, kStageModal, kStageRecorder,
 
 int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes);
 int build_pml_maps(Ctx* ctx);
+cudaError_t launch_mma(Ctx* ctx, int k, cudaStream_t s);
 void free_ctx_device(Ctx* ctx);
 template <typename T>
 int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, bool fork, cudaEvent_t* ev);

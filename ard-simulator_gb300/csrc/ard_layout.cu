@@ -256,11 +256,11 @@ void build_mma_jobs(Ctx* ctx, Take take) {
   auto table = [&](int n) {
     auto it = tab.find(n);
     if (it != tab.end()) return it->second;
-    const long long o = take(4LL * mma_table_elems(n));
+    const long long o = take(8LL * mma_table_elems(n));
     tab[n] = o;
     return o;
   };
-  for (int k = 0; k < 4; ++k) { ctx->mjobs[k].clear(); ctx->mtiles[k] = 0; }
+  for (int k = 0; k < 8; ++k) { ctx->mjobs[k].clear(); ctx->mtiles[k] = 0; }
   auto add = [&](int list, MmaJob j) {
     mma_ntile(j.N, &j.nt, &j.bn);
     j.nch = (j.K + kMmaBK - 1) / kMmaBK;
@@ -273,16 +273,17 @@ void build_mma_jobs(Ctx* ctx, Take take) {
     ctx->mjobs[list].push_back(j);
   };
   for (const DctDev& D : ctx->dct) {
-    struct Axis { long long f, p, P, R, tmp; int nU, nV, ld; };
-    const Axis axes[3] = {{D.fX, D.pX, D.PX, D.RX, D.tmpX, D.h, D.d, D.h},
-                          {D.fY, D.pY, D.PY, D.RY, D.tmpY, D.w, D.d, D.wp},
-                          {D.fZ, D.pZ, D.PZ, D.RZ, D.tmpZ, D.w, D.h, D.wp}};
+    struct Axis { long long f, p, P, R, tmp, q, adj; int nU, nV, ld; };
+    const Axis axes[3] = {{D.fX, D.pX, D.PX, D.RX, D.tmpX, D.qX, D.aX, D.h, D.d, D.h},
+                          {D.fY, D.pY, D.PY, D.RY, D.tmpY, D.qY, D.aY, D.w, D.d, D.wp},
+                          {D.fZ, D.pZ, D.PZ, D.RZ, D.tmpZ, D.qZ, D.aZ, D.w, D.h, D.wp}};
     for (const Axis& a : axes) {
       const long long LS = (long long)a.nV * a.ld;
       const int Vp = (a.nV + 3) & ~3;
       const long long TS = (long long)a.nU * Vp;   // one transposed intermediate
       const long long tU = table(a.nU), tV = table(a.nV);
-      const long long SU = mma_table_elems(a.nU), SV = mma_table_elems(a.nV);   // Chi, Clo, CiThi, CiTlo each
+      // Chi, Clo, CiThi, CiTlo, CThi, CTlo, Cihi, Cilo: mma_table_elems each
+      const long long SU = mma_table_elems(a.nU), SV = mma_table_elems(a.nV);
       MmaJob f1{}, f2{}, i1{}, i2{};
       f1.nout = f2.nout = i1.nout = i2.nout = 6;
       for (int o = 0; o < 6; ++o) {
@@ -306,6 +307,24 @@ void build_mma_jobs(Ctx* ctx, Take take) {
       i2.R = a.nU; i2.ldb = Vp; i2.K = i2.N = a.nV; i2.thi = tV + 2 * SV; i2.tlo = tV + 3 * SV;
       i2.ldo = a.ld; i2.scale = (float)D.si;
       add(0, f1); add(1, f2); add(2, i1); add(3, i2);
+      if (ctx->adjoint) {
+        // the adjoint step's transposes: the adjoint face pressure q through
+        // the transposed inverse (passes 1, 2: the forward passes' form with
+        // Ci in place of C, scale s_i), the summed contraction partials R
+        // through the transposed forward (passes 3, 4: the inverse passes'
+        // form with C^T in place of Ci^T, scale s_f) into the adjoint force
+        MmaJob a1 = f1, a2 = f2, a3 = i1, a4 = i2;
+        for (int o = 0; o < 6; ++o) {
+          const int n = o % 3;
+          a1.in0[o] = a.q + n * LS; a1.in1[o] = a.q + (5 - n) * LS;
+          a4.out[o] = a.adj + o * LS;
+        }
+        a1.thi = tU + 6 * SU; a1.tlo = tU + 7 * SU;
+        a2.thi = tV + 6 * SV; a2.tlo = tV + 7 * SV; a2.scale = (float)D.si;
+        a3.thi = tU + 4 * SU; a3.tlo = tU + 5 * SU;
+        a4.thi = tV + 4 * SV; a4.tlo = tV + 5 * SV; a4.scale = (float)D.sf;
+        add(4, a1); add(5, a2); add(6, a3); add(7, a4);
+      }
     }
   }
   ctx->mma_tables.assign(tab.begin(), tab.end());
@@ -965,8 +984,8 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
   if ((rc = up(&ctx->d_fwd2d, ctx->fwd2d))) return rc;
   if ((rc = up(&ctx->d_inv2d, ctx->inv2d))) return rc;
   if ((rc = up(&ctx->d_psum, ctx->psum))) return rc;
-  for (int k = 0; k < 4; ++k)
-    if (ctx->mma_faces && (rc = up(&ctx->d_mjobs[k], ctx->mjobs[k]))) return rc;
+  for (int k = 0; k < 8; ++k)
+    if (ctx->mma_faces && !ctx->mjobs[k].empty() && (rc = up(&ctx->d_mjobs[k], ctx->mjobs[k]))) return rc;
   ARD_CUDA(cudaMalloc(&ctx->d_err, sizeof(int)));
   ARD_CUDA(cudaMemset(ctx->d_err, 0, sizeof(int)));
   if (int rc = build_pml_maps(ctx)) return rc;
@@ -1036,6 +1055,7 @@ void free_ctx_device(Ctx* ctx) {
                   ctx->d_hist, ctx->d_t, ctx->d_adj1_2d, ctx->d_adj2_2d, ctx->d_adjg[0], ctx->d_adjg[1],
                   ctx->d_adjg[2], ctx->d_adjg[3], ctx->d_tb, ctx->d_phist, ctx->d_psum,
                   ctx->d_cell_iface, ctx->d_mjobs[0], ctx->d_mjobs[1], ctx->d_mjobs[2], ctx->d_mjobs[3],
+                  ctx->d_mjobs[4], ctx->d_mjobs[5], ctx->d_mjobs[6], ctx->d_mjobs[7],
                   ctx->d_err, ctx->d_pml_maps};
   for (void* p : ptrs)
     if (p) cudaFree(p);

@@ -441,10 +441,13 @@ static __global__ void __launch_bounds__(kMmaThreads, 1) face_mma_kernel(MmaArgs
 }
 
 // FP64 -> split TF32 transform tables of the tensor-core passes for extent n,
-// pre-tiled (mma_ntile): forward C[k][j] = 2 cos(pi (j + 1/2) k / n) with the
-// output k as row, and inverse Ci^T[j][k] = Ci[k][j] (row k = 0 of Ci
-// halved) with the output j as row; each as hi / lo.  Layout at off: Chi,
-// Clo, CiThi, CiTlo, mma_table_elems(n) each.
+// pre-tiled (mma_ntile), each as hi / lo, with the output index as row:
+//   C    [k][j] = 2 cos(pi (j + 1/2) k / n)           forward (REDFT10)
+//   Ci^T [j][k] = Ci[k][j], Ci = C with row k = 0 halved  inverse (REDFT01)
+//   C^T  [j][k] = C[k][j]                             adjoint of the forward
+//   Ci   [k][j]                                       adjoint of the inverse
+// Layout at off: Chi, Clo, CiThi, CiTlo, CThi, CTlo, Cihi, Cilo,
+// mma_table_elems(n) each.
 static __global__ void mma_table_kernel(float* buf, long long off, int n) {
   int nt, bn;
   mma_ntile(n, &nt, &bn);
@@ -459,22 +462,24 @@ static __global__ void mma_table_kernel(float* buf, long long off, int n) {
     const int ic = (int)(blk % nch), it = (int)(blk / nch);
     const int row = it * bn + r, col = ic * kMmaBK + k;
     const long long dst = (blk * bn + r) * kMmaBK + ((((k >> 2) ^ r) & 7) << 2) + (k & 3);
-    double c = 0.0, ci = 0.0;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};   // C, Ci^T, C^T, Ci at (row, col)
     if (row < n && col < n) {
       const long long q = ((long long)(2 * col + 1) * row) % (4LL * n);    // C[row][col]: k = row, j = col
-      c = 2.0 * cospi((double)q / (2.0 * n));
-      const long long q2 = ((long long)(2 * row + 1) * col) % (4LL * n);   // Ci[col][row]: k = col, j = row
-      ci = 2.0 * cospi((double)q2 / (2.0 * n));
-      if (col == 0) ci *= 0.5;
+      const double c = 2.0 * cospi((double)q / (2.0 * n));
+      const long long q2 = ((long long)(2 * row + 1) * col) % (4LL * n);   // C[col][row]: k = col, j = row
+      const double ct = 2.0 * cospi((double)q2 / (2.0 * n));
+      v[0] = c;
+      v[1] = col == 0 ? 0.5 * ct : ct;
+      v[2] = ct;
+      v[3] = row == 0 ? 0.5 * c : c;
     }
-    const uint32_t ch = tf32_rna((float)c);
-    const uint32_t cl = tf32_rna((float)(c - (double)__uint_as_float(ch)));
-    const uint32_t ih = tf32_rna((float)ci);
-    const uint32_t il = tf32_rna((float)(ci - (double)__uint_as_float(ih)));
-    buf[off + dst] = __uint_as_float(ch);
-    buf[off + S + dst] = __uint_as_float(cl);
-    buf[off + 2 * S + dst] = __uint_as_float(ih);
-    buf[off + 3 * S + dst] = __uint_as_float(il);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const uint32_t h = tf32_rna((float)v[t]);
+      const uint32_t l = tf32_rna((float)(v[t] - (double)__uint_as_float(h)));
+      buf[off + (2 * t) * S + dst] = __uint_as_float(h);
+      buf[off + (2 * t + 1) * S + dst] = __uint_as_float(l);
+    }
   }
 }
 

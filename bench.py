@@ -29,7 +29,9 @@ advanced one time step; PML cells are extra work, not counted.
           per launch from the ncu summary in profiles/
   stage_roofline  every stage against its bound: PML 44 B per PML cell,
           interfaces 48 B per face cell, modal 28 B per air cell (HBM), the
-          face transforms as useful FLOP/s
+          face transforms as useful FLOP/s (and, on the tensor-core path, the
+          split-TF32 product rate against the dense TF32 rate) and as bytes
+          moved against HBM
   reference_arithmetic  the same workload in the reference's FP32
           arithmetic (the mode that reproduces the reference CPU solver's
           rounding), timed the same way on a shorter run
@@ -121,6 +123,33 @@ def face_flops(scenes):
             macs = d * h * (d + h) + d * w * (d + w) + h * w * (h + w)
             total += 2 * 2 * 6 * macs
     return total
+
+
+def face_bytes(scenes):
+    """Algorithmic bytes of one step's four face-transform passes (FP32): each
+    pass reads its input layers and writes its output layers once, the first
+    pass of each direction reading the two layers of every pair (forward:
+    the force faces, inverse: the contraction sums): 2 + 1 + 1 (forward) and
+    2 + 1 + 1 (inverse) reads plus 4 writes of the 18 face layers."""
+    total = 0
+    for sc in scenes:
+        for p in sc.partitions:
+            if p[0] != 0:
+                continue
+            w, h, d = p[5], p[6], p[7]
+            fe = 6 * (d * h + d * w + h * w)
+            total += 4 * 10 * fe
+    return total
+
+
+def tf32_peak_tflops():
+    """Dense TF32 tensor rate: half the measured dense bf16 rate (the
+    tensor cores' TF32 rate is half their bf16 rate)."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]) / 2, "measured bf16 / 2"
+    return 1900.0 / 2, "fallback bf16 / 2"
 
 
 class ClockSampler:
@@ -573,12 +602,24 @@ def main():
     f_ms = stages["fwd_rows"] + stages["fwd_cols"] + stages["inv_cols"] + stages["inv_rows"]
     flops = face_flops(prof_scenes)
     f_tf = flops / (f_ms / 1e3) / 1e12 if f_ms > 0 else 0.0
+    tensor = "faces tensor-core" in sim.layout
+    if tensor:
+        # split TF32: three products per useful one, on the tensor cores
+        tpk, tpk_src = tf32_peak_tflops()
+        f_compute = {"path": "tcgen05 split TF32 (3 products per useful MAC)", "tensor_tflops": 3 * f_tf,
+                     "tf32_peak_tflops": tpk, "tf32_peak_source": tpk_src, "frac_of_tf32_peak": 3 * f_tf / tpk}
+    else:
+        f_compute = {"path": "CUDA-core FP32", "fp32_fma_peak_tflops": FP32_FMA_TFLOPS,
+                     "frac_of_fp32_fma_peak": f_tf / FP32_FMA_TFLOPS}
+    f_bytes = face_bytes(prof_scenes)
     stage_roofline = {
         "modal": hbm_stage(modal_ms, BYTES_PER_AIR_CELL * p_air),
         "pml": hbm_stage(stages["pml"], BYTES_PER_PML_CELL * p_pml),
         "iface": hbm_stage(stages["iface"], BYTES_PER_FACE_CELL * p_face),
-        "faces": {"ms": f_ms, "useful_flops": flops, "achieved_tflops": f_tf,
-                  "fp32_fma_peak_tflops": FP32_FMA_TFLOPS, "frac_of_fp32_fma_peak": f_tf / FP32_FMA_TFLOPS},
+        "faces": dict({"ms": f_ms, "useful_flops": flops, "achieved_tflops": f_tf,
+                       "algorithmic_bytes": f_bytes,
+                       "achieved_gbs": f_bytes / (f_ms / 1e3) / 1e9 if f_ms > 0 else 0.0,
+                       "frac_of_hbm": (f_bytes / (f_ms / 1e3) / 1e9 / peak) if f_ms > 0 else 0.0}, **f_compute),
         "recorder_and_sums": {"ms": stages["recorder"]},
         "peak_gbs": peak, "peak_source": peak_kind,
     }

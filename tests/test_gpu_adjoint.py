@@ -177,6 +177,31 @@ def test_fp32_gradients_follow_fp64():
         assert rel(g32["p0"][k], g64["p0"][k]) < 2e-3
 
 
+def test_fp32_tensor_core_adjoint(monkeypatch):
+    """FP32 with the face transforms forced onto the two-pass form: the
+    forward's and the adjoint's face passes run on the tensor cores (split
+    TF32).  Gradients within 1e-4 relative L2 of the same FP32 problem on the
+    fused CUDA-core face kernel, and within the FP32 bar of FP64."""
+    def rel(a, b):
+        a = np.asarray(a, np.float64); b = np.asarray(b, np.float64)
+        return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+    g64 = Problem(precision=A.PREC_F64, seed=5).grads(checkpoint_every=20)
+    fused = Problem(precision=A.PREC_F32, seed=5)
+    assert "faces fused" in fused.sim.layout
+    gf = fused.grads(checkpoint_every=20)
+    monkeypatch.setenv("ARD_FACE_TWO_PASS", "1")
+    mma = Problem(precision=A.PREC_F32, seed=5)
+    assert "faces tensor-core" in mma.sim.layout
+    gm = mma.grads(checkpoint_every=20)
+    for key in ("grad_source", "grad_scale"):
+        assert rel(gm[key], gf[key]) < 1e-4, key
+        assert rel(gm[key], g64[key]) < 2e-3, key
+    for k in range(len(AIR)):
+        assert rel(gm["p0"][k], gf["p0"][k]) < 1e-4, k
+        assert rel(gm["p0"][k], g64["p0"][k]) < 2e-3, k
+
+
 def test_adjoint_errors():
     scene = A.build_scene(AIR, SOURCES, RECORDERS, DH, DT, C0, PML)
     plain = A.Simulation(scene, precision=A.PREC_F64, max_steps=T_STEPS)
