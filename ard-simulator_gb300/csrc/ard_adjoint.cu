@@ -5,12 +5,19 @@
 //
 // The step is linear in its state (modal levels, shell forces, PML fields),
 // so the adjoint recursion needs no forward state except for the damping
-// gradient, whose terms multiply forward PML values.  Without that gradient
-// the call is one forward run (recorder residuals) and one backward run.
-// With it, the forward run stores a copy of the state block every K steps;
-// the backward run then works through the segments last to first, each one
-// recomputed from its checkpoint while the PML pressure and phi_n of every
-// step are kept, then swept backwards.
+// gradient, whose terms multiply forward PML values (p(t), p(t-1), phi_n(t)).
+// Without that gradient the call is one forward run (recorder residuals)
+// and one backward run.  With it the forward PML values come back in
+// reverse order by one of:
+//   - the whole PML history, kept in the forward run when it fits;
+//   - segments of K steps swept backwards from the last.  A segment's PML
+//     history is made again before its backward sweep, either by PML replay
+//     (the forward run recorded the interfaces' forcing of the PML strips
+//     for its steps and kept its PML state at its start: the PML runs again
+//     on its own) or by recompute (the forward run kept the whole state at
+//     its start: the whole segment runs again).  The trailing segments are
+//     replayed, as many as the forcing record allows in the free memory, and
+//     the ones before them recomputed.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -40,7 +47,7 @@ struct AdjBuffers {
   void* resid = nullptr;      // [T][n_rec_total] residuals (context precision)
   double* gsrc = nullptr;     // [T][n_src_total]
   double* gz = nullptr;       // [pml blocks][kMaxPmlLayers]
-  void* ckpt = nullptr;       // [n_ckpt + 1][state or PML state] (last: after step T)
+  void* ckpt = nullptr;       // segment checkpoints and the state after step T (adjoint_impl)
   void* hist_p = nullptr;     // [K + 1][region]
   void* hist_phn = nullptr;   // [K][region]
   void* fhist = nullptr;      // [T][strip region] (PML replay)
@@ -244,63 +251,81 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
   const long long hlen = ctx->pml_region[0][1] - ctx->pml_region[0][0];
   // How the forward PML values reach the backward sweep (damping gradient only):
   //   kFull     the whole history p(t), phi_n(t) kept in one forward run
-  //   kReplay   the strip forcing of every step and a copy of the PML state every
-  //             K steps are kept; each segment's PML runs again on its own
-  //   kRecompute  a copy of the whole state every K steps; each segment runs again
-  enum { kNone, kFull, kReplay, kRecompute } mode = kNone;
-  long long K = T_steps, n_ckpt = 1;
+  //   kSegments the run in segments of K steps, the backward sweep segment by
+  //             segment from the last; a segment's history comes back either
+  //             by replay (its strip forcing recorded in the forward run and
+  //             the PML state kept at its start: the PML runs again on its
+  //             own) or by recompute (the whole state kept at its start: the
+  //             whole segment runs again).  The first n_rc segments are
+  //             recomputed and the rest replayed, n_rc as small as the memory
+  //             allows: 0 (all replayed) where the forcing record fits.
+  enum { kNone, kFull, kSegments } mode = kNone;
+  long long K = T_steps, n_seg = 1, n_rc = 0;
   const long long pml_begin = ctx->pml_region[0][0];
   const long long pml_len = ctx->state_end - pml_begin;       // PML fields + strip forces
   const long long flen = ctx->state_end - ctx->force_begin;    // strip forces
   AdjBuffers ab;
+  // memory of a segmented run (elements): history of one segment, PML
+  // checkpoints of the replayed segments, whole-state checkpoints of the
+  // recomputed ones, the state after T (whole, or its PML part where nothing
+  // is recomputed), the forcing record of the replayed steps
+  auto seg_need = [&](long long k, long long nrc) {
+    const long long ns = (T_steps + k - 1) / k;
+    const long long t_rep = std::max(0LL, T_steps - nrc * k);
+    return (2 * k + 1) * hlen + (ns - nrc) * pml_len + (nrc > 0 ? (nrc + 1) * state_len : pml_len) + t_rep * flen;
+  };
   if (need_hist) {
     size_t free_b = 0, total_b = 0;
     ARD_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const size_t budget = free_b / 10 * 9;
-    const size_t full = (size_t)(2 * T_steps + 1) * hlen * es;
+    const long long budget = (long long)(free_b / 10 * 9 / es);
+    const long long full = (2 * T_steps + 1) * hlen;
     auto segment_k = [&](long long ckpt_len) {
-      // balance checkpoint memory (n_ckpt copies) against history memory (2 K PML regions)
+      // balance checkpoint memory (one copy per segment) against history memory (2 K PML regions)
       const double k = std::sqrt((double)T_steps * (double)ckpt_len / (2.0 * (double)std::max(1LL, hlen)));
       return std::max(1LL, std::min(T_steps, (long long)std::ceil(k)));
     };
-    // ARD_ADJOINT_RECOMPUTE=1 (tests): the segment-recompute path even where the replay fits
+    // ARD_ADJOINT_RECOMPUTE=1 (tests): every segment recomputed; =n (n > 1): the first n - 1
     const char* force_rc = std::getenv("ARD_ADJOINT_RECOMPUTE");
-    const bool recompute_only = force_rc && force_rc[0] == '1';
-    if (checkpoint_every <= 0 && full <= free_b / 2 && !recompute_only) {
+    const long long forced = force_rc ? std::atoll(force_rc) : 0;
+    if (checkpoint_every <= 0 && (size_t)full * es <= free_b / 2 && forced <= 0) {
       mode = kFull;
     } else {
+      mode = kSegments;
       K = checkpoint_every > 0 ? std::min<long long>(checkpoint_every, T_steps) : segment_k(pml_len);
-      n_ckpt = (T_steps + K - 1) / K;
-      const size_t replay = ((size_t)T_steps * flen + (size_t)(n_ckpt + 1) * pml_len + (size_t)(2 * K + 1) * hlen) * es;
-      if (replay <= budget && !recompute_only) {
-        mode = kReplay;
-      } else {
+      n_seg = (T_steps + K - 1) / K;
+      if (forced > 0 || seg_need(K, 0) > budget) {
         if (checkpoint_every <= 0) K = segment_k(state_len);
-        n_ckpt = (T_steps + K - 1) / K;
-        mode = kRecompute;
+        n_seg = (T_steps + K - 1) / K;
+        if (forced == 1) {
+          n_rc = n_seg;
+        } else if (forced > 1) {
+          n_rc = std::min(n_seg, forced - 1);
+        } else {
+          n_rc = 1;
+          while (n_rc < n_seg && seg_need(K, n_rc) > budget) ++n_rc;
+        }
       }
+      if (seg_need(K, n_rc) > budget) {
+        ctx->err = "ard_adjoint: checkpoints and PML history need " + std::to_string((seg_need(K, n_rc) * es) >> 20) +
+                   " MiB (segments of " + std::to_string(K) + " steps, " + std::to_string(n_rc) +
+                   " recomputed); " + std::to_string(free_b >> 20) + " MiB free";
+        return ARD_ERR_OOM;
+      }
+      const long long n_rep = n_seg - n_rc;
+      ARD_CUDA(cudaMalloc(&ab.ckpt, std::max<size_t>(1, (size_t)(n_rep * pml_len + (n_rc > 0 ? (n_rc + 1) * state_len : pml_len)) * es)));
+      if (n_rep > 0) ARD_CUDA(cudaMalloc(&ab.fhist, std::max<size_t>(1, (size_t)(T_steps - n_rc * K) * flen * es)));
     }
-    if (mode != kFull) n_ckpt = (T_steps + K - 1) / K;
-    size_t need = (size_t)(2 * K + 1) * hlen * es;
-    if (mode == kReplay) need += ((size_t)T_steps * flen + (size_t)(n_ckpt + 1) * pml_len) * es;
-    if (mode == kRecompute) need += (size_t)(n_ckpt + 1) * state_len * es;
-    if (need > budget) {
-      ctx->err = "ard_adjoint: checkpoints and PML history need " + std::to_string(need >> 20) + " MiB (" +
-                 std::to_string(n_ckpt) + " checkpoints every " + std::to_string(K) + " steps); " +
-                 std::to_string(free_b >> 20) + " MiB free";
-      return ARD_ERR_OOM;
-    }
-    if (mode == kReplay) {
-      ARD_CUDA(cudaMalloc(&ab.ckpt, (size_t)(n_ckpt + 1) * pml_len * es));
-      ARD_CUDA(cudaMalloc(&ab.fhist, std::max<size_t>(1, (size_t)T_steps * flen * es)));
-    }
-    if (mode == kRecompute) ARD_CUDA(cudaMalloc(&ab.ckpt, (size_t)(n_ckpt + 1) * state_len * es));
-    ARD_CUDA(cudaMalloc(&ab.hist_p, (size_t)(K + 1) * hlen * es));
-    ARD_CUDA(cudaMalloc(&ab.hist_phn, (size_t)K * hlen * es));
+    const long long hk = mode == kFull ? T_steps : K;
+    ARD_CUDA(cudaMalloc(&ab.hist_p, (size_t)(hk + 1) * hlen * es));
+    ARD_CUDA(cudaMalloc(&ab.hist_phn, (size_t)hk * hlen * es));
   }
-  ctx->adj_mode = mode == kFull ? "whole PML history" : mode == kReplay ? "PML replay" :
-                  mode == kRecompute ? "segment recompute" : "no forward values";
-  ctx->adj_k = mode == kReplay || mode == kRecompute ? K : 0;
+  ctx->adj_mode = mode == kFull ? "whole PML history"
+                 : mode == kNone ? "no forward values"
+                 : n_rc == 0     ? "PML replay"
+                 : n_rc == n_seg ? "segment recompute"
+                                 : "hybrid: segment recompute for the first " + std::to_string(n_rc) + " of " +
+                                       std::to_string(n_seg) + " segments, PML replay after them";
+  ctx->adj_k = mode == kSegments ? K : 0;
   const int nrec = ctx->n_rec_total, nsrc = ctx->n_src_total;
   ARD_CUDA(cudaMalloc(&ab.resid, std::max<size_t>(1, (size_t)T_steps * nrec * es)));
   ARD_CUDA(cudaMalloc(&ab.gsrc, std::max<size_t>(1, (size_t)T_steps * nsrc * sizeof(double))));
@@ -311,14 +336,21 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
   T* buf = reinterpret_cast<T*>(ctx->d_buf);
   T* state = buf + ctx->state_begin;
   T* pml_state = buf + pml_begin;
-  const long long ckpt_len = mode == kReplay ? pml_len : state_len;
-  T* ckpt_src = mode == kReplay ? pml_state : state;
-  auto ckpt = [&](long long i) { return reinterpret_cast<T*>(ab.ckpt) + i * ckpt_len; };
+  const long long t_rc = n_rc * K;   // steps [0, t_rc) recomputed, [t_rc, T) replayed
+  // checkpoint storage: whole states of the recomputed segments' starts, then
+  // the state after T (whole where anything is recomputed, else its PML
+  // part), then the PML states of the replayed segments' starts
+  T* ckbase = reinterpret_cast<T*>(ab.ckpt);
+  auto full_ckpt = [&](long long i) { return ckbase + i * state_len; };
+  T* final_ckpt = ckbase + n_rc * state_len;
+  const long long final_len = n_rc > 0 ? state_len : pml_len;
+  T* final_src = n_rc > 0 ? state : pml_state;
+  auto pml_ckpt = [&](long long i) { return final_ckpt + final_len + (i - n_rc) * pml_len; };
 
   // What the PML kernel records or replays (PmlHist): p(t), phi_n(t) of
   // steps t0 <= t < t1 (the slot of p(t0 - 1) filled here from the state
-  // before step t0), the strip forcing of steps [ft0, ft1), and the forcing
-  // it replays.
+  // before step t0), the strip forcing of the replayed steps [t_rc, T), and
+  // the forcing it replays.
   T* hp = reinterpret_cast<T*>(ab.hist_p);
   T* hphn = reinterpret_cast<T*>(ab.hist_phn);
   T* fh = reinterpret_cast<T*>(ab.fhist);
@@ -330,22 +362,25 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
       ARD_CUDA(cudaMemcpyAsync(hp, buf + ctx->pml_region[q_prev][0], hlen * es, cudaMemcpyDeviceToDevice, s));
     }
     h.flen = flen;
-    if (rec_force) { h.f = fh; h.ft0 = 0; h.ft1 = T_steps; }
-    if (replay) { h.fsrc = fh; h.fs0 = 0; }
+    if (rec_force) { h.f = fh; h.ft0 = t_rc; h.ft1 = T_steps; }
+    if (replay) { h.fsrc = fh; h.fs0 = t_rc; }
     ARD_CUDA(cudaMemcpyAsync(ctx->d_phist, &h, sizeof(h), cudaMemcpyHostToDevice, s));
     return ARD_OK;
   };
 
   // ---- forward run ----
   ard_ctx* handle = reinterpret_cast<ard_ctx*>(ctx);
-  if (mode == kReplay || mode == kRecompute) {
-    if (mode == kReplay && (rc = set_hist(false, 0, 0, true, false))) return rc;
-    for (long long i = 0; i < n_ckpt; ++i) {
-      ARD_CUDA(cudaMemcpyAsync(ckpt(i), ckpt_src, ckpt_len * es, cudaMemcpyDeviceToDevice, s));
+  if (mode == kSegments) {
+    if (n_seg > n_rc && (rc = set_hist(false, 0, 0, true, false))) return rc;   // record the replayed steps' forcing
+    for (long long i = 0; i < n_seg; ++i) {
+      if (i < n_rc)
+        ARD_CUDA(cudaMemcpyAsync(full_ckpt(i), state, state_len * es, cudaMemcpyDeviceToDevice, s));
+      else
+        ARD_CUDA(cudaMemcpyAsync(pml_ckpt(i), pml_state, pml_len * es, cudaMemcpyDeviceToDevice, s));
       rc = ard_step(handle, std::min(K, T_steps - i * K), nullptr);
       if (rc) return rc;
     }
-    ARD_CUDA(cudaMemcpyAsync(ckpt(n_ckpt), ckpt_src, ckpt_len * es, cudaMemcpyDeviceToDevice, s));
+    ARD_CUDA(cudaMemcpyAsync(final_ckpt, final_src, final_len * es, cudaMemcpyDeviceToDevice, s));
     if ((rc = set_hist(false, 0, 0, false, false))) return rc;
   } else {
     if (mode == kFull && (rc = set_hist(true, 0, T_steps, false, false))) return rc;
@@ -381,15 +416,19 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
   ARD_CUDA(cudaMemsetAsync(buf + ctx->adj_begin, 0, adj_len * es, s));
   const HistView hv = need_hist ? HistView{ab.hist_p, ab.hist_phn, hlen, ab.gz} : HistView{};
   AdjGraph graph;   // captured on first use, for this call's buffers
-  if (mode == kReplay || mode == kRecompute) {
-    for (long long i = n_ckpt - 1; i >= 0; --i) {
+  if (mode == kSegments) {
+    for (long long i = n_seg - 1; i >= 0; --i) {
       const long long t0 = i * K, t1 = std::min(T_steps, t0 + K);
-      // run the segment again from its checkpoint, keeping its PML history
-      ARD_CUDA(cudaMemcpyAsync(ckpt_src, ckpt(i), ckpt_len * es, cudaMemcpyDeviceToDevice, s));
+      const bool replay = i >= n_rc;
+      // the segment again from its checkpoint, keeping its PML history
+      if (replay)
+        ARD_CUDA(cudaMemcpyAsync(pml_state, pml_ckpt(i), pml_len * es, cudaMemcpyDeviceToDevice, s));
+      else
+        ARD_CUDA(cudaMemcpyAsync(state, full_ckpt(i), state_len * es, cudaMemcpyDeviceToDevice, s));
       set_step_counter_kernel<<<1, 32, 0, s>>>(ctx->d_t, t0);
       ARD_CUDA(cudaGetLastError());
-      if ((rc = set_hist(true, t0, t1, false, mode == kReplay))) return rc;
-      if (mode == kReplay) {
+      if ((rc = set_hist(true, t0, t1, false, replay))) return rc;
+      if (replay) {
         // the PML on its own, driven by the recorded strip forcing
         for (long long t = t0; t < t1; ++t)
           if ((rc = launch_pml<T>(ctx, (int)(t & 1), (int)(t - t0), s))) return rc;
@@ -403,7 +442,7 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
       if (rc) return rc;
     }
     // leave the forward state as after step T
-    ARD_CUDA(cudaMemcpyAsync(ckpt_src, ckpt(n_ckpt), ckpt_len * es, cudaMemcpyDeviceToDevice, s));
+    ARD_CUDA(cudaMemcpyAsync(final_src, final_ckpt, final_len * es, cudaMemcpyDeviceToDevice, s));
     set_step_counter_kernel<<<1, 32, 0, s>>>(ctx->d_t, T_steps);
     ARD_CUDA(cudaGetLastError());
     ctx->t_host = T_steps;

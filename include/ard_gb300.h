@@ -357,13 +357,15 @@ int ard_read_field_noalloc(ard_ctx* ctx, int32_t scene, int32_t partition, float
  *   loss         1 float per scene
  * grad_scale needs forward PML values in reverse order.  With
  * checkpoint_every <= 0 the whole PML history is kept when it fits in half
- * the free device memory.  Otherwise (or with checkpoint_every > 0) the
- * forward run keeps the interfaces' forcing of the PML strips for every step
- * and a copy of the PML state every K steps (K = checkpoint_every, or chosen
- * to balance the memories), and each segment's PML runs again on its own
- * before its backward sweep; where even that does not fit, a copy of the
- * whole state every K steps and the whole segment runs again.  Without
- * grad_scale nothing is stored.  ard_describe names the path taken.
+ * the free device memory.  Otherwise (or with checkpoint_every > 0) the run
+ * is cut into segments of K steps (K = checkpoint_every, or chosen to
+ * balance the memories) swept backwards from the last; for the trailing
+ * segments the forward run keeps the interfaces' forcing of the PML strips
+ * and the PML state at each segment's start, and the segment's PML runs
+ * again on its own before its backward sweep; for the leading segments,
+ * where the forcing record does not fit in the free memory, it keeps the
+ * whole state at each segment's start and the whole segment runs again.
+ * Without grad_scale nothing is stored.  ard_describe names the path taken.
  * dJ/d(initial pressure) of an air partition is read afterwards with
  * ard_read_initial_pressure_grad (width*height*depth floats, [z][y][x]). */
 int ard_adjoint(ard_ctx* ctx, int64_t T, const float* target,

@@ -142,6 +142,14 @@ def test_checkpoint_interval_does_not_change_gradients(problem, monkeypatch):
     assert "segment recompute" in problem.sim.layout
     np.testing.assert_allclose(g["grad_scale"], problem.g["grad_scale"], rtol=1e-10, atol=0)
     np.testing.assert_allclose(g["grad_source"], problem.g["grad_source"], rtol=1e-10, atol=1e-30)
+    # the hybrid: the first two of nine segments recomputed, the rest replayed
+    monkeypatch.setenv("ARD_ADJOINT_RECOMPUTE", "3")
+    g = problem.grads(checkpoint_every=9)
+    assert "hybrid" in problem.sim.layout and "first 2 of 9" in problem.sim.layout
+    np.testing.assert_allclose(g["grad_scale"], problem.g["grad_scale"], rtol=1e-10, atol=0)
+    np.testing.assert_allclose(g["grad_source"], problem.g["grad_source"], rtol=1e-10, atol=1e-30)
+    for k in range(len(AIR)):
+        np.testing.assert_allclose(g["p0"][k], problem.g["p0"][k], rtol=1e-10, atol=1e-30)
     monkeypatch.delenv("ARD_ADJOINT_RECOMPUTE")
     # without the damping gradient nothing is checkpointed: the other gradients stay
     g = problem.grads(want_scale=False)
