@@ -51,8 +51,9 @@ struct AdjBuffers {
   void* hist_p = nullptr;     // [K + 1][region]
   void* hist_phn = nullptr;   // [K][region]
   void* fhist = nullptr;      // [T][strip region] (PML replay)
+  CUtensorMap* hmaps = nullptr;   // tensor maps of hist_p per slab (the adjoint PML kernel's p(t) tiles)
   ~AdjBuffers() {
-    void* ptrs[] = {resid, gsrc, gz, ckpt, hist_p, hist_phn, fhist};
+    void* ptrs[] = {resid, gsrc, gz, ckpt, hist_p, hist_phn, fhist, hmaps};
     for (void* p : ptrs)
       if (p) cudaFree(p);
   }
@@ -76,6 +77,7 @@ struct HistView {
   const void* phn = nullptr;
   long long hlen = 0;
   double* gz = nullptr;
+  const CUtensorMap* hmaps = nullptr;
 };
 
 // One adjoint step t (tstep: position inside the launch sequence, counted
@@ -102,7 +104,7 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
   if (!ctx->pml_blocks.empty()) {
     PmlAdjArgs<T> pa{buf, ctx->d_pml, ctx->d_pml_blocks, (int)ctx->pml_blocks.size(), lin, ly, lout, (t + 1) & 1,
                      (T)ctx->dt, (T)ctx->dh, (T)ctx->c0, (const T*)hv.p, (const T*)hv.phn, hv.hlen, ctx->d_tb,
-                     tstep, hv.gz};
+                     tstep, hv.gz, ctx->d_pml_amaps, hv.hmaps, ctx->d_err};
     ARD_CUDA(launch_dep(pml_adjoint_kernel<T>, grid_for((long long)ctx->pml_blocks.size(), 1, ctx->num_sms * 8), 256,
                         0, fork ? s2 : s, pa));
     ARD_CUDA(cudaGetLastError());
@@ -318,6 +320,7 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
     const long long hk = mode == kFull ? T_steps : K;
     ARD_CUDA(cudaMalloc(&ab.hist_p, (size_t)(hk + 1) * hlen * es));
     ARD_CUDA(cudaMalloc(&ab.hist_phn, (size_t)hk * hlen * es));
+    if ((rc = build_pml_hist_maps(ctx, ab.hist_p, hlen, hk + 1, &ab.hmaps))) return rc;
   }
   ctx->adj_mode = mode == kFull ? "whole PML history"
                  : mode == kNone ? "no forward values"
@@ -414,7 +417,7 @@ int adjoint_impl(Ctx* ctx, long long T_steps, const float* target, int checkpoin
   // ---- backward run ----
   const long long adj_len = ctx->adj_end - ctx->adj_begin;
   ARD_CUDA(cudaMemsetAsync(buf + ctx->adj_begin, 0, adj_len * es, s));
-  const HistView hv = need_hist ? HistView{ab.hist_p, ab.hist_phn, hlen, ab.gz} : HistView{};
+  const HistView hv = need_hist ? HistView{ab.hist_p, ab.hist_phn, hlen, ab.gz, ab.hmaps} : HistView{};
   AdjGraph graph;   // captured on first use, for this call's buffers
   if (mode == kSegments) {
     for (long long i = n_seg - 1; i >= 0; --i) {

@@ -144,6 +144,27 @@ struct PmlAdjArgs {
   const long long* tc;  // {t of the first step of the launch sequence, t0}
   int tstep;
   double* gz;           // [nblocks][kMaxPmlLayers] damping-gradient sums (accumulated)
+  const CUtensorMap* amaps;   // per slab: ap[0..2], apha[0..1], aphb[0..1] as [L][A][B] tensors
+  const CUtensorMap* hmaps;   // per slab: the history of p as a [K+1][L][A][B] tensor (null: no gradient)
+  int* err;                   // set to 1 when a bounded wait runs out
+};
+
+// The adjoint PML kernel's tile boxes per layer (each 128-byte aligned in the
+// stage): X = adjoint p(t+1) with a halo of 3 (x from b0 - 4), Phi_a with a
+// halo of 2 along a, Phi_b with a halo of 2 along b (x from b0 - 4), and for
+// the damping gradient the forward p(t) with a halo of 2 along both (x from
+// b0 - 4).
+template <typename T>
+struct PmlAdjStage {
+  static constexpr int PW = kPmlTB + 8;
+  static constexpr int xs = (kPmlTA + 6) * PW * (int)sizeof(T);
+  static constexpr int xsa = (xs + 127) & ~127;
+  static constexpr int fa = (kPmlTA + 4) * kPmlTB * (int)sizeof(T);
+  static constexpr int fb = kPmlTA * PW * (int)sizeof(T);
+  static constexpr int fba = (fb + 127) & ~127;
+  static constexpr int qs = (kPmlTA + 4) * PW * (int)sizeof(T);
+  static constexpr int qsa = (qs + 127) & ~127;
+  static constexpr int bytes = xsa + fa + fba + qsa;
 };
 
 // With X = adjoint p(t+1), Y = adjoint p(t+2), Phi = adjoint phi(t+1) and
@@ -158,13 +179,13 @@ struct PmlAdjArgs {
 //   dJ/dz(l) += sum over layer l of  -dt X (p(t) - p(t-1))
 //               - dt Phi_n (phi_n(t) + Dn p(t)) + dt Phi_a Da p(t) + dt Phi_b Db p(t)
 template <typename T>
-__global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
+__global__ void __launch_bounds__(256, 4) pml_adjoint_kernel(PmlAdjArgs<T> a) {
   grid_dependency_wait();
-  constexpr int TA = 8, TB = 32;
-  __shared__ T Xs[TA + 6][TB + 6];
-  __shared__ T FA[TA + 4][TB];
-  __shared__ T FB[TA][TB + 4];
-  __shared__ T Qs[TA + 4][TB + 4];
+  using S = PmlAdjStage<T>;
+  constexpr int TA = kPmlTA, TB = kPmlTB, PW = S::PW;
+  __shared__ __align__(128) unsigned char stage[2][S::bytes];
+  __shared__ uint64_t bar[2];
+  __shared__ volatile int s_abort;
   __shared__ double red[8][kMaxPmlLayers];
   const T c7[7] = {2, -27, 270, -490, 270, -27, 2};
   const T c5[5] = {1, -8, 0, 8, -1};
@@ -176,12 +197,49 @@ __global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
     const long long t = a.tc[0] - a.tstep;
     hofs = t - a.tc[1];   // hist_p[hofs + 1] = p(t), hist_p[hofs] = p(t-1), hist_phn[hofs] = phi_n(t)
   }
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init_fence();
+    s_abort = 0;
+  }
+  __syncthreads();
+  // thread 0's issue cursor over the block's (tile, layer) sequence, one layer
+  // ahead of the computation: X, Phi_a, Phi_b (and p(t)) boxes of the layer
+  int ibi = blockIdx.x, il = 0, iL = 0;
+  uint32_t issued = 0;
+  const uint32_t tx = (uint32_t)(S::xs + S::fa + S::fb + (zgrad ? S::qs : 0));
+  auto issue_next = [&]() {
+    if (ibi >= a.nblocks) return;
+    const int4 blk = a.blocks[ibi];
+    if (il == 0) iL = a.pml[blk.x].L;
+    const CUtensorMap* mp = a.amaps + 7LL * blk.x;
+    const int sg = (int)(issued & 1);
+    unsigned char* sb = stage[sg];
+    mbar_arrive_expect_tx(&bar[sg], tx);
+    tma_load_3d(sb, mp + a.lx, blk.z - 4, blk.y - 3, il, &bar[sg]);
+    tma_load_3d(sb + S::xsa, mp + 3 + a.fin, blk.z, blk.y - 2, il, &bar[sg]);
+    tma_load_3d(sb + S::xsa + S::fa, mp + 5 + a.fin, blk.z - 4, blk.y, il, &bar[sg]);
+    if (zgrad) tma_load_4d(sb + S::xsa + S::fa + S::fba, a.hmaps + blk.x, blk.z - 4, blk.y - 2, il, (int)(hofs + 1), &bar[sg]);
+    ++issued;
+    if (++il == iL) {
+      il = 0;
+      ibi += gridDim.x;
+    }
+  };
+  if (threadIdx.x == 0) {
+    issue_next();
+    issue_next();
+  }
+  uint32_t used = 0;
+  bool stop = false;
   const T dt = a.dt, dt2 = a.dt * a.dt;
   const T r180 = (T)1 / ((T)180 * a.dh * a.dh), r12 = (T)1 / ((T)12 * a.dh);
-  for (int bi = blockIdx.x; bi < a.nblocks; bi += gridDim.x) {
+  for (int bi = blockIdx.x; bi < a.nblocks && !stop; bi += gridDim.x) {
     const int4 blk = a.blocks[bi];
     const PmlDev& P = a.pml[blk.x];
     const int L = P.L, A = P.A, B = P.B, Bp = P.Bp;
+    const long long hoff = P.hoff;   // in registers: the layer loop stores through the pool pointer
     const int a0 = blk.y, b0 = blk.z;
     const int ia = a0 + ta, ib = b0 + tb;
     const bool inside = ia < A && ib < B;
@@ -191,15 +249,13 @@ __global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
     T* Y = a.buf + P.ap[a.ly];
     T* O = a.buf + P.ap[a.lo];
     const T* Fn = a.buf + P.aphn[a.fin];
-    const T* Fa = a.buf + P.apha[a.fin];
-    const T* Fb = a.buf + P.aphb[a.fin];
     T* Fn_o = a.buf + P.aphn[a.fin ^ 1];
     T* Fa_o = a.buf + P.apha[a.fin ^ 1];
     T* Fb_o = a.buf + P.aphb[a.fin ^ 1];
     const T* zeta = a.buf + P.zeta;
-    const T* hp = zgrad ? a.hist_p + (hofs + 1) * a.hlen + P.hoff : nullptr;    // p(t)
-    const T* hpp = zgrad ? a.hist_p + hofs * a.hlen + P.hoff : nullptr;         // p(t-1)
-    const T* hfn = zgrad ? a.hist_phn + hofs * a.hlen + P.hoff : nullptr;       // phi_n(t)
+    const T* hp = zgrad ? a.hist_p + (hofs + 1) * a.hlen + hoff : nullptr;    // p(t)
+    const T* hpp = zgrad ? a.hist_p + hofs * a.hlen + hoff : nullptr;         // p(t-1)
+    const T* hfn = zgrad ? a.hist_phn + hofs * a.hlen + hoff : nullptr;       // phi_n(t)
     // register windows along the normal: X(l-3 .. l+3), z Phi_n(l-2 .. l+2), p(t)(l-2 .. l+2)
     T xw[7], zw[5], qw[5];
 #pragma unroll
@@ -214,88 +270,46 @@ __global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
       zw[m] = ok ? zeta[ll] * Fn[ll * lstride + col] : (T)0;
       qw[m] = (ok && zgrad) ? hp[ll * lstride + col] : (T)0;
     }
-    __syncthreads();  // the previous tile's layer sums have been read
-    if (threadIdx.x < 8 * kMaxPmlLayers) red[threadIdx.x / kMaxPmlLayers][threadIdx.x % kMaxPmlLayers] = 0;
-    // the next layer's tiles and point values, fetched while the current layer computes
-    T nX[3], nA[2], nB[2], nQ[2], ny = 0, no = 0, nfn = 0, npp = 0, nhf = 0;
+    if (zgrad) {
+      if (threadIdx.x < 8 * kMaxPmlLayers) red[threadIdx.x / kMaxPmlLayers][threadIdx.x % kMaxPmlLayers] = 0;
+      __syncthreads();   // cleared before any warp adds its first layer sum
+    }
+    // the next layer's point values, fetched while the current layer computes
+    T ny = 0, no = 0, nfn = 0, npp = 0, nhf = 0;
     auto fetch = [&](int l) {
-      const T* Xl = X + l * lstride;
-      const T* fal = Fa + l * lstride;
-      const T* fbl = Fb + l * lstride;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const int i = threadIdx.x + 256 * k;
-        const int r = i / (TB + 6), c = i - r * (TB + 6);
-        const int aa = a0 + r - 3, bb = b0 + c - 3;
-        nX[k] = (i < (TA + 6) * (TB + 6) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? Xl[(long long)aa * Bp + bb] : (T)0;
-      }
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int i = threadIdx.x + 256 * k;
-        const int r = i / TB, c = i - r * TB;
-        const int aa = a0 + r - 2, bb = b0 + c;
-        nA[k] = (i < (TA + 4) * TB && aa >= 0 && aa < A && bb < B) ? fal[(long long)aa * Bp + bb] : (T)0;
-      }
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int i = threadIdx.x + 256 * k;
-        const int r = i / (TB + 4), c = i - r * (TB + 4);
-        const int aa = a0 + r, bb = b0 + c - 2;
-        nB[k] = (i < TA * (TB + 4) && aa < A && bb >= 0 && bb < B) ? fbl[(long long)aa * Bp + bb] : (T)0;
-      }
       const long long I = l * lstride + col;
       ny = inside ? Y[I] : (T)0;
       no = inside ? O[I] : (T)0;
       nfn = inside ? Fn[I] : (T)0;
       if (zgrad) {
-        const T* hpl = hp + l * lstride;
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          const int i = threadIdx.x + 256 * k;
-          const int r = i / (TB + 4), c = i - r * (TB + 4);
-          const int aa = a0 + r - 2, bb = b0 + c - 2;
-          nQ[k] = (i < (TA + 4) * (TB + 4) && aa >= 0 && aa < A && bb >= 0 && bb < B) ? hpl[(long long)aa * Bp + bb]
-                                                                                        : (T)0;
-        }
         npp = inside ? hpp[I] : (T)0;
         nhf = inside ? hfn[I] : (T)0;
       }
     };
-    auto commit = [&]() {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const int i = threadIdx.x + 256 * k;
-        if (i < (TA + 6) * (TB + 6)) Xs[i / (TB + 6)][i % (TB + 6)] = nX[k];
-      }
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int i = threadIdx.x + 256 * k;
-        if (i < (TA + 4) * TB) FA[i / TB][i % TB] = nA[k];
-        if (i < TA * (TB + 4)) FB[i / (TB + 4)][i % (TB + 4)] = nB[k];
-        if (zgrad && i < (TA + 4) * (TB + 4)) Qs[i / (TB + 4)][i % (TB + 4)] = nQ[k];
-      }
-    };
     fetch(0);
     for (int l = 0; l < L; ++l) {
-      __syncthreads();  // previous layer done with the tiles
-      commit();
+      const int sg = (int)(used & 1);
+      mbar_wait_bounded(&bar[sg], (used >> 1) & 1, &s_abort);
+      const T* Xs = reinterpret_cast<const T*>(stage[sg]);                                  // [TA + 6][PW]
+      const T* FA = reinterpret_cast<const T*>(stage[sg] + S::xsa);                         // [TA + 4][TB]
+      const T* FB = reinterpret_cast<const T*>(stage[sg] + S::xsa + S::fa);                 // [TA][PW]
+      const T* Qs = reinterpret_cast<const T*>(stage[sg] + S::xsa + S::fa + S::fba);        // [TA + 4][PW]
       const T y0 = ny, o0 = no, fn0 = nfn, pp0 = npp, hf0 = nhf;
       if (l + 1 < L) fetch(l + 1);
-      __syncthreads();
       T g = 0;
-      if (inside) {
+      if (inside && !s_abort) {
         T lx = 0;
 #pragma unroll
-        for (int m = 0; m < 7; ++m) lx += c7[m] * (xw[m] + Xs[ta + m][tb + 3] + Xs[ta + 3][tb + m]);
+        for (int m = 0; m < 7; ++m) lx += c7[m] * (xw[m] + Xs[(ta + m) * PW + tb + 4] + Xs[(ta + 3) * PW + tb + 1 + m]);
         T dnx = 0, dax = 0, dbx = 0, dnz = 0, daf = 0, dbf = 0;
 #pragma unroll
         for (int m = 0; m < 5; ++m) {
           dnx += c5[m] * xw[m + 1];
-          dax += c5[m] * Xs[ta + 1 + m][tb + 3];
-          dbx += c5[m] * Xs[ta + 3][tb + 1 + m];
+          dax += c5[m] * Xs[(ta + 1 + m) * PW + tb + 4];
+          dbx += c5[m] * Xs[(ta + 3) * PW + tb + 2 + m];
           dnz += c5[m] * zw[m];
-          daf += c5[m] * FA[ta + m][tb];
-          dbf += c5[m] * FB[ta][tb + m];
+          daf += c5[m] * FA[(ta + m) * TB + tb];
+          dbf += c5[m] * FB[ta * PW + tb + 2 + m];
         }
         lx *= r180;
         dnx *= r12; dax *= r12; dbx *= r12;
@@ -303,7 +317,7 @@ __global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
         const long long I = l * lstride + col;
         const T zn = zeta[l];
         const T x0 = xw[3];
-        const T fa0 = FA[ta + 2][tb], fb0 = FB[ta][tb + 2];
+        const T fa0 = FA[(ta + 2) * TB + tb], fb0 = FB[ta * PW + tb + 4];
         O[I] = o0 + (T)2 * x0 + dt2 * a.c0 * a.c0 * lx - dt * zn * x0 + (dt * zn - (T)1) * y0 + dt * dnz -
                dt * zn * (daf + dbf);
         Y[I] = 0;
@@ -315,16 +329,18 @@ __global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
 #pragma unroll
           for (int m = 0; m < 5; ++m) {
             dnp += c5[m] * qw[m];
-            dap += c5[m] * Qs[ta + m][tb + 2];
-            dbp += c5[m] * Qs[ta + 2][tb + m];
+            dap += c5[m] * Qs[(ta + m) * PW + tb + 4];
+            dbp += c5[m] * Qs[(ta + 2) * PW + tb + 2 + m];
           }
           dnp *= r12; dap *= r12; dbp *= r12;
           g = -dt * x0 * (qw[2] - pp0) - dt * fn0 * (hf0 + dnp) + dt * (fa0 * dap + fb0 * dbp);
         }
       }
       if (zgrad) {
-        const double sw = warp_sum((double)g);
-        if (lane == 0) red[warp][l] += sw;
+        // the warp's sum in the working type (FP64 arithmetic is scarce on
+        // this GPU), the block's sums over warps and tiles in double
+        const T sw = warp_sum(g);
+        if (lane == 0) red[warp][l] += (double)sw;
       }
       // slide the windows one layer
 #pragma unroll
@@ -335,15 +351,34 @@ __global__ void __launch_bounds__(256, 2) pml_adjoint_kernel(PmlAdjArgs<T> a) {
       const bool ok3 = inside && l + 3 < L;
       zw[4] = ok3 ? zeta[l + 3] * Fn[(l + 3) * lstride + col] : (T)0;
       qw[4] = (ok3 && zgrad) ? hp[(l + 3) * lstride + col] : (T)0;
+      __syncthreads();   // every thread is done with stage sg
+      if (s_abort) {
+        stop = true;
+        break;
+      }
+      if (threadIdx.x == 0) issue_next();
+      ++used;
     }
+    if (stop) break;
     if (zgrad) {
-      __syncthreads();
       if (threadIdx.x < L) {
         double sum = 0;
         for (int w8 = 0; w8 < 8; ++w8) sum += red[w8][threadIdx.x];
         a.gz[(long long)bi * kMaxPmlLayers + threadIdx.x] += sum;
       }
+      __syncthreads();   // the layer sums are read before the next tile clears them
     }
+  }
+  if (s_abort) {
+    // a wait ran out: report it, and give loads still in flight time to land
+    // (bounded) before the block's shared memory is released
+    if (threadIdx.x == 0) {
+      atomicExch(a.err, 1);
+      const long long t0 = clock64();
+      while (clock64() - t0 < 20000000LL) {
+      }
+    }
+    __syncthreads();
   }
 }
 

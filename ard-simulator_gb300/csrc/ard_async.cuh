@@ -75,6 +75,16 @@ __device__ __forceinline__ void tma_load_3d(void* smem, const CUtensorMap* map, 
       : "memory");
 }
 
+// The same for a 4D tensor map (coordinates x, y, z, w).
+__device__ __forceinline__ void tma_load_4d(void* smem, const CUtensorMap* map, int x, int y, int z, int w,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(smem)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // generic-proxy shared-memory writes -> visible to the async proxy (tensor cores, TMA)
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 

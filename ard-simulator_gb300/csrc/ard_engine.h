@@ -148,6 +148,7 @@ struct Ctx {
   MmaJob* d_mjobs[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   int* d_err = nullptr;           // set by a kernel whose bounded wait ran out (checked on synchronize)
   CUtensorMap* d_pml_maps = nullptr;   // tensor maps of the PML tile loads (build_pml_maps)
+  CUtensorMap* d_pml_amaps = nullptr;  // the adjoint PML kernel's (options.adjoint)
 
   // neighbourhood recording (ard_record_neighbourhoods): the 10 x 10 x 10
   // pressure cube around every recorder after every step, [max_steps][n_rec_total][1000]
@@ -169,6 +170,7 @@ enum { kStagePml = 0, kStageFwdRows, kStageFwdCols, kStageModal, kStageRecorder,
 
 int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes);
 int build_pml_maps(Ctx* ctx);
+int build_pml_hist_maps(Ctx* ctx, const void* hist, long long hlen, long long slots, CUtensorMap** out);
 cudaError_t launch_mma(Ctx* ctx, int k, cudaStream_t s);
 void free_ctx_device(Ctx* ctx);
 template <typename T>

@@ -1056,7 +1056,7 @@ void free_ctx_device(Ctx* ctx) {
                   ctx->d_adjg[2], ctx->d_adjg[3], ctx->d_tb, ctx->d_phist, ctx->d_psum,
                   ctx->d_cell_iface, ctx->d_mjobs[0], ctx->d_mjobs[1], ctx->d_mjobs[2], ctx->d_mjobs[3],
                   ctx->d_mjobs[4], ctx->d_mjobs[5], ctx->d_mjobs[6], ctx->d_mjobs[7],
-                  ctx->d_err, ctx->d_pml_maps};
+                  ctx->d_err, ctx->d_pml_maps, ctx->d_pml_amaps};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
@@ -1084,39 +1084,81 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
-// The tensor maps of the PML kernel's tile loads: per slab p, phi_a and phi_b
-// of both time levels as [L][A][B] tensors (row pitch Bp), with the box of
-// the tile each one feeds (PmlStage).  Elements outside the tensor read as
-// zero, the reference's sentinel.
-int build_pml_maps(Ctx* ctx) {
-  if (ctx->pml.empty()) return ARD_OK;
+// One PML slab field as a [L][A][B] tensor (row pitch Bp) at `base`, or with
+// `slots` > 0 as [slots][L][A][B] with `slot_stride` elements between slots,
+// read in boxes of box_b x box_a (x 1 x 1).  Elements outside the tensor read
+// as zero, the reference's sentinel.
+static int encode_slab_map(Ctx* ctx, CUtensorMap* map, const PmlDev& P, const void* base, cuuint32_t box_b,
+                           cuuint32_t box_a, long long slots = 0, long long slot_stride = 0) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) { ctx->err = "cuTensorMapEncodeTiled is not available from the driver"; return ARD_ERR_CUDA; }
   const size_t es = elem_size(ctx);
   const CUtensorMapDataType type =
       ctx->prec == ARD_PREC_F64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-  const cuuint32_t boxes[3][3] = {{(cuuint32_t)kPmlTB + 8, (cuuint32_t)kPmlTA + 6, 1},   // p: halo 3 (b from b0 - 4)
-                                  {(cuuint32_t)kPmlTB, (cuuint32_t)kPmlTA + 4, 1},       // phi_a: halo 2 along a
-                                  {(cuuint32_t)kPmlTB + 8, (cuuint32_t)kPmlTA, 1}};      // phi_b: halo 2 along b
-  const cuuint32_t estr[3] = {1, 1, 1};
-  std::vector<CUtensorMap> maps(6 * ctx->pml.size());
+  const cuuint32_t rank = slots > 0 ? 4 : 3;
+  const cuuint64_t dims[4] = {(cuuint64_t)P.B, (cuuint64_t)P.A, (cuuint64_t)P.L, (cuuint64_t)std::max(1LL, slots)};
+  const cuuint64_t strides[3] = {(cuuint64_t)P.Bp * es, (cuuint64_t)P.A * P.Bp * es, (cuuint64_t)slot_stride * es};
+  const cuuint32_t box[4] = {box_b, box_a, 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = enc(map, type, rank, const_cast<void*>(base), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    ctx->err = "cuTensorMapEncodeTiled failed for a PML slab (error " + std::to_string((int)r) + ")";
+    return ARD_ERR_CUDA;
+  }
+  return ARD_OK;
+}
+
+// The tensor maps of the PML kernels' tile loads, with the box of the tile
+// each one feeds (PmlStage, PmlAdjStage): per slab p (halo 3, x from b0 - 4),
+// phi_a (halo 2 along a) and phi_b (halo 2 along b, x from b0 - 4) of both
+// time levels; with the adjoint also its three levels of p and two of each
+// phi.
+int build_pml_maps(Ctx* ctx) {
+  if (ctx->pml.empty()) return ARD_OK;
+  const size_t es = elem_size(ctx);
+  const cuuint32_t PW = kPmlTB + 8;
+  char* base = (char*)ctx->d_buf;
+  std::vector<CUtensorMap> maps(6 * ctx->pml.size()), amaps(ctx->adjoint ? 7 * ctx->pml.size() : 0);
   for (size_t k = 0; k < ctx->pml.size(); ++k) {
     const PmlDev& P = ctx->pml[k];
-    const cuuint64_t dims[3] = {(cuuint64_t)P.B, (cuuint64_t)P.A, (cuuint64_t)P.L};
-    const cuuint64_t strides[2] = {(cuuint64_t)P.Bp * es, (cuuint64_t)P.A * P.Bp * es};
     const long long offs[6] = {P.p[0], P.p[1], P.pha[0], P.pha[1], P.phb[0], P.phb[1]};
-    for (int q = 0; q < 6; ++q) {
-      const CUresult r = enc(&maps[6 * k + q], type, 3, (char*)ctx->d_buf + offs[q] * es, dims, strides, boxes[q / 2],
-                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if (r != CUDA_SUCCESS) {
-        ctx->err = "cuTensorMapEncodeTiled failed for a PML slab (error " + std::to_string((int)r) + ")";
-        return ARD_ERR_CUDA;
-      }
+    const cuuint32_t bb[3] = {PW, (cuuint32_t)kPmlTB, PW}, ba[3] = {kPmlTA + 6, kPmlTA + 4, kPmlTA};
+    for (int q = 0; q < 6; ++q)
+      if (int rc = encode_slab_map(ctx, &maps[6 * k + q], P, base + offs[q] * es, bb[q / 2], ba[q / 2])) return rc;
+    if (ctx->adjoint) {
+      const long long aoffs[7] = {P.ap[0], P.ap[1], P.ap[2], P.apha[0], P.apha[1], P.aphb[0], P.aphb[1]};
+      const int kind[7] = {0, 0, 0, 1, 1, 2, 2};
+      for (int q = 0; q < 7; ++q)
+        if (int rc = encode_slab_map(ctx, &amaps[7 * k + q], P, base + aoffs[q] * es, bb[kind[q]], ba[kind[q]]))
+          return rc;
     }
   }
   ARD_CUDA(cudaMalloc(&ctx->d_pml_maps, sizeof(CUtensorMap) * maps.size()));
   ARD_CUDA(cudaMemcpy(ctx->d_pml_maps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
+  if (ctx->adjoint) {
+    ARD_CUDA(cudaMalloc(&ctx->d_pml_amaps, sizeof(CUtensorMap) * amaps.size()));
+    ARD_CUDA(cudaMemcpy(ctx->d_pml_amaps, amaps.data(), sizeof(CUtensorMap) * amaps.size(), cudaMemcpyHostToDevice));
+  }
+  return ARD_OK;
+}
+
+// Tensor maps of a PML history buffer (`slots` copies of the all-slab p
+// region, `hlen` elements apart) for the adjoint PML kernel's p(t) tiles:
+// per slab a [slots][L][A][B] tensor read in boxes of the p(t) tile.
+int build_pml_hist_maps(Ctx* ctx, const void* hist, long long hlen, long long slots, CUtensorMap** out) {
+  *out = nullptr;
+  if (ctx->pml.empty()) return ARD_OK;
+  const size_t es = elem_size(ctx);
+  std::vector<CUtensorMap> maps(ctx->pml.size());
+  for (size_t k = 0; k < ctx->pml.size(); ++k) {
+    const PmlDev& P = ctx->pml[k];
+    if (int rc = encode_slab_map(ctx, &maps[k], P, (const char*)hist + P.hoff * es, kPmlTB + 8, kPmlTA + 4, slots, hlen))
+      return rc;
+  }
+  ARD_CUDA(cudaMalloc(out, sizeof(CUtensorMap) * maps.size()));
+  ARD_CUDA(cudaMemcpy(*out, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
   return ARD_OK;
 }
 
