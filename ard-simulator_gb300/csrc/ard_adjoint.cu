@@ -92,7 +92,7 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
     ARD_CUDA(cudaMemsetAsync(buf + ctx->q_begin, 0, sizeof(T) * (size_t)(ctx->q_end - ctx->q_begin), s));
   if (ctx->n_face_cells > 0) {
     IfaceAdjArgs<T> ia{buf, ctx->d_ifs, (int)ctx->ifs.size(), ctx->n_face_cells, ctx->d_dct, ctx->d_pml,
-                       ctx->d_mask, lin, lout, (T)ctx->c0, (T)ctx->dh, (T)ctx->dt};
+                       ctx->d_mask, lin, lout, (T)ctx->c0, (T)ctx->dh, (T)ctx->dt, ctx->d_cell_iface};
     ARD_CUDA(launch_dep(iface_adjoint_kernel<T>, grid_for(ctx->n_face_cells, 256, ctx->num_sms * 16), 256, 0, s, ia));
     ARD_CUDA(cudaGetLastError());
   }

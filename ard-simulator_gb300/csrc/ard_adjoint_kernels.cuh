@@ -40,6 +40,7 @@ struct IfaceAdjArgs {
   int lin;    // level of the adjoint PML pressure of step t + 1 (the strip force enters p(t + 1) times dt^2)
   int lout;   // level of the adjoint PML pressure of step t (accumulated)
   T c0, dh, dt;
+  const int* cell_iface;   // interface of every face cell
 };
 
 // Adjoint of the force value that the forward step writes at crossing
@@ -58,22 +59,21 @@ __device__ __forceinline__ T adj_force(const IfaceAdjArgs<T>& a, int type, const
   return a.dt * a.dt * a.buf[P.ap[a.lin] + ((long long)c * P.A + v) * P.Bp + u];
 }
 
+// Offset of the adjoint pressure value of crossing coordinate c, face
+// coordinates (u, v) of side s (the cell the forward step read the pressure
+// of).
 template <typename T>
-__device__ __forceinline__ void adj_pressure_add(const IfaceAdjArgs<T>& a, int type, const SideDev& s, int c, int u,
-                                                 int v, T val) {
-  if (val == (T)0) return;
+__device__ __forceinline__ long long adj_pressure_offset(const IfaceAdjArgs<T>& a, int type, const SideDev& s, int c,
+                                                         int u, int v) {
   if (s.kind == 0) {
     const DctDev& D = a.dct[s.idx];
     const int layer = face_layer(c, s.ext);
-    long long o;
-    if (type == 0) o = D.qX + ((long long)layer * D.d + v) * D.h + u;
-    else if (type == 1) o = D.qY + ((long long)layer * D.d + v) * D.wp + u;
-    else o = D.qZ + ((long long)layer * D.h + v) * D.wp + u;
-    atomicAdd(a.buf + o, val);
-    return;
+    if (type == 0) return D.qX + ((long long)layer * D.d + v) * D.h + u;
+    if (type == 1) return D.qY + ((long long)layer * D.d + v) * D.wp + u;
+    return D.qZ + ((long long)layer * D.h + v) * D.wp + u;
   }
   const PmlDev& P = a.pml[s.idx];
-  atomicAdd(a.buf + P.ap[a.lout] + ((long long)c * P.A + v) * P.Bp + u, val);
+  return P.ap[a.lout] + ((long long)c * P.A + v) * P.Bp + u;
 }
 
 // Transpose of iface_kernel: every force value the forward step writes
@@ -86,12 +86,7 @@ __global__ void __launch_bounds__(256) iface_adjoint_kernel(IfaceAdjArgs<T> a) {
                      {2, -27, 270, -270, 27, -2}, {0, 2, -27, 27, -2, 0},     {0, 0, 2, -2, 0, 0}};
   for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < a.total;
        g += (long long)gridDim.x * blockDim.x) {
-    int lo = 0, hi = a.nif - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (a.ifs[mid].cell0 <= g) lo = mid; else hi = mid - 1;
-    }
-    const IfaceDev& I = a.ifs[lo];
+    const IfaceDev& I = a.ifs[a.cell_iface[g]];
     const long long local = g - I.cell0;
     const int nu = I.u1 - I.u0;
     const int iu = I.u0 + (int)(local % nu);
@@ -114,10 +109,18 @@ __global__ void __launch_bounds__(256) iface_adjoint_kernel(IfaceAdjArgs<T> a) {
         if (use_hi) gh[n] += g * C[m + 3][3 + n];
       }
     }
+    // every target offset first, the atomics after them: descriptor fields
+    // read after an atomic through the pool pointer would be loaded again
+    long long ol[3], oh[3];
 #pragma unroll
     for (int n = 0; n < 3; ++n) {
-      adj_pressure_add(a, I.type, I.lo, I.lo.ext - 3 + n, lu, lv, gl[n]);
-      adj_pressure_add(a, I.type, I.hi, n, hu, hv, gh[n]);
+      ol[n] = adj_pressure_offset(a, I.type, I.lo, I.lo.ext - 3 + n, lu, lv);
+      oh[n] = adj_pressure_offset(a, I.type, I.hi, n, hu, hv);
+    }
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+      if (gl[n] != (T)0) atomicAdd(a.buf + ol[n], gl[n]);
+      if (gh[n] != (T)0) atomicAdd(a.buf + oh[n], gh[n]);
     }
   }
 }
