@@ -65,9 +65,11 @@ int configure_adjoint(Ctx* ctx) {
   const int msmem = (int)(kModalSmemElems * sizeof(T));
   ARD_CUDA(cudaFuncSetAttribute(modal_kernel<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, msmem));
   ARD_CUDA(cudaFuncSetAttribute(modal_kernel<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, msmem));
-  if (ctx->fused_faces)
-    ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  std::max(ctx->smem_optin, (int)ctx->f2d_bytes)));
+  if (ctx->fused_faces) {
+    const int f2d = std::max(ctx->smem_optin, (int)ctx->f2d_bytes);
+    ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, f2d));
+    ARD_CUDA(cudaFuncSetAttribute(face2d_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, f2d));
+  }
   ARD_CUDA(configure_face_gemm<T>());
   return ARD_OK;
 }
@@ -112,8 +114,8 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
   if (!ctx->dct.empty()) {
     const int gx = ctx->num_sms * 4;
     if (ctx->fused_faces) {
-      ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for((long long)ctx->adj1_2d.size(), 1, gx), kFace2DThreads,
-                          ctx->f2d_bytes, s, buf, ctx->d_adj1_2d, (int)ctx->adj1_2d.size(), ctx->f2d_smem));
+      ARD_CUDA(launch_face2d<T>(ctx->adj1_split, (long long)ctx->adj1_2d.size() / 2, gx, ctx->f2d_bytes, s, buf,
+                                ctx->d_adj1_2d, ctx->f2d_smem));
     } else if (ctx->mma_faces) {
       ARD_CUDA(launch_mma(ctx, 4, s));
       ARD_CUDA(launch_mma(ctx, 5, s));
@@ -140,8 +142,8 @@ int launch_adjoint_step(Ctx* ctx, int t, int tstep, cudaStream_t s, cudaStream_t
     }
     if (int rc2 = launch_post_modal<T>(ctx, s, 0, false)) return rc2;
     if (ctx->fused_faces) {
-      ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for((long long)ctx->adj2_2d.size(), 1, gx), kFace2DThreads,
-                          ctx->f2d_bytes, s, buf, ctx->d_adj2_2d, (int)ctx->adj2_2d.size(), ctx->f2d_smem));
+      ARD_CUDA(launch_face2d<T>(ctx->adj2_split, (long long)ctx->adj2_2d.size() / 2, gx, ctx->f2d_bytes, s, buf,
+                                ctx->d_adj2_2d, ctx->f2d_smem));
     } else if (ctx->mma_faces) {
       ARD_CUDA(launch_mma(ctx, 6, s));
       ARD_CUDA(launch_mma(ctx, 7, s));

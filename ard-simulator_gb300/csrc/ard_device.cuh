@@ -160,7 +160,8 @@ struct Face2DJob {
   int V, U, ld;
   int u0, ub;
   int which;     // 0: both outputs; 1: out0 only; 2: out1 only (a pair split over two blocks)
-  int narrow;    // 1: at most 16 columns, two rows per lane pair
+  int narrow;    // 1: at most 16 columns (16 rows per warp)
+  int split;     // 1: the rows are split between the two CTAs of the cluster
   int part;      // air partition (engine index)
   double scale;
 };

@@ -101,13 +101,17 @@ static int configure_kernels(Ctx* ctx) {
   if (ctx->prec == ARD_PREC_F64) {
     ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
     ARD_CUDA(cudaFuncSetAttribute(modal_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
-    if (ctx->fused_faces)
+    if (ctx->fused_faces) {
       ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, f2d));
+      ARD_CUDA(cudaFuncSetAttribute(face2d_cluster_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, f2d));
+    }
   } else {
     ARD_CUDA(cudaFuncSetAttribute(modal_kernel<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
     ARD_CUDA(cudaFuncSetAttribute(modal_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, modal_smem));
-    if (ctx->fused_faces)
+    if (ctx->fused_faces) {
       ARD_CUDA(cudaFuncSetAttribute(face2d_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, f2d));
+      ARD_CUDA(cudaFuncSetAttribute(face2d_cluster_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, f2d));
+    }
   }
   ARD_CUDA(ctx->prec == ARD_PREC_F64 ? configure_face_gemm<double>() : configure_face_gemm<float>());
   if (ctx->mma_faces)
@@ -350,9 +354,8 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
       if (k == kStageFwdRows) {
         if (ctx->fused_faces) {
           const int n = G.f_hi - G.f_lo;
-          if (n > 0)
-            ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st, buf,
-                                ctx->d_fwd2d + G.f_lo, n, ctx->f2d_smem));
+          ARD_CUDA(launch_face2d<T>(G.f_split, n, gx, ctx->f2d_bytes, st, buf, ctx->d_fwd2d + 2 * G.f_lo,
+                                    ctx->f2d_smem));
         } else if (ctx->mma_faces) {
           ARD_CUDA(launch_mma(ctx, 0, st));
         } else {
@@ -383,9 +386,8 @@ int launch_step(Ctx* ctx, int par, int tstep, cudaStream_t s, cudaStream_t s2, b
       } else if (k == kStageInvCols) {
         if (ctx->fused_faces) {
           const int n = G.i_hi - G.i_lo;
-          if (n > 0)
-            ARD_CUDA(launch_dep(face2d_kernel<T>, grid_for(n, 1, gx), kFace2DThreads, ctx->f2d_bytes, st, buf,
-                                ctx->d_inv2d + G.i_lo, n, ctx->f2d_smem));
+          ARD_CUDA(launch_face2d<T>(G.i_split, n, gx, ctx->f2d_bytes, st, buf, ctx->d_inv2d + 2 * G.i_lo,
+                                    ctx->f2d_smem));
         } else if (ctx->mma_faces) {
           ARD_CUDA(launch_mma(ctx, 2, st));
         } else {

@@ -81,6 +81,7 @@ struct Ctx {
   struct AirGroup {
     int part_lo = 0, part_hi = 0;
     int f_lo = 0, f_hi = 0, i_lo = 0, i_hi = 0;
+    bool f_split = false, i_split = false;   // the range holds row-split face jobs (cluster launch)
     int t_lo = 0, t_hi = 0, r_lo = 0, r_hi = 0, s_lo = 0, s_hi = 0;
     long long s_first = 0, s_total = 0;
   };
@@ -116,6 +117,7 @@ struct Ctx {
   // adjoint face transforms (options.adjoint): fused 2D jobs and the two-pass
   // GEMM form (q rows, q columns, R columns, R rows)
   std::vector<Face2DJob> adj1_2d, adj2_2d;
+  bool adj1_split = false, adj2_split = false;
   JobList adjg[4];
   long long q_begin = 0, q_end = 0;          // adjoint face pressure (zeroed every adjoint step)
   bool adj_valid = false;                    // adjoint levels hold mu(0), mu(1) of the last ard_adjoint

@@ -25,6 +25,7 @@
 // whole-field transforms of the readouts and the initial pressure.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -603,198 +604,309 @@ __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
   }
 }
 
-constexpr int kFace2DThreads = 512;
+constexpr int kFace2DThreads = 256;
+constexpr int kFace2DWarps = kFace2DThreads / 32;
 
 struct Face2DSmem {
-  int xs;  // X0 and later A: max(V * xp, V * ap)
-  int x1;  // X1: V * xp
-  int bs;  // B slab, column-major: 32 * face2d_pitch(U)
-  int ts;  // each of T0, T1, column-major: 32 * face2d_pitch(V)
+  int xs;  // X0: max over the jobs of V * max(xp, ap) (the layer, then E or the A table)
+  int x1;  // X1: the same (the second layer, then O or the A table)
+  int bs;  // B slab, row-major [Up][32]
+  int ts;  // each of T0, T1, row-major [Vp][32]
 };
 
-// Column pitch of the column-major slab arrays: 4 mod 8 elements, so the 128-bit
-// loads of a quarter warp (8 columns) hit distinct bank groups.
+// Row pitch of the staged layers and of the staged A table: 4 mod 8 elements,
+// so rows r .. r + 7 start in distinct 16-byte bank groups.
 __host__ __device__ inline int face2d_pitch(int n) {
   const int n4 = (n + 3) & ~3;
   return n4 + ((n4 & 7) ? 8 : 4);
 }
 
-// One block per (layer pair, 32-column slab): X0, X1 (V x U, row pitch ld)
-// are staged in shared memory with cp.async, combined into E = X0 + X1 and
-// O = X0 - X1, transformed along U for the slab (T = E B, O B) and then along
-// V, giving out0 = scale A (E B) and out1 = scale A (O B) for the slab.
-// Layer pairs are the two layers of the same distance from either face
+// One block per (layer pair, slab of at most 32 columns).  X0, X1 (V x U, row
+// pitch ld) are staged in shared memory (cp.async) and combined into
+// E = X0 + X1 and O = X0 - X1; then along U, T = E B and O B over the slab
+// (B: U x U table, its slab row-major), and along V, out0 = scale A (E B),
+// out1 = scale A (O B) (A: V x V table, row o contiguous).  Layer pairs are
+// the two layers of the same distance from either face
 // (C(k, n-1-j) = (-1)^k C(k, j)): forward (and the adjoint of the inverse)
 // take the layers and give the even / odd parts, the inverse (and the
 // adjoint of the forward) take the even / odd parts and give the layers.
-template <typename T>
-__global__ void __launch_bounds__(kFace2DThreads) face2d_kernel(T* __restrict__ buf, const Face2DJob* __restrict__ jobs,
-                                                      int njobs, Face2DSmem sm) {
+//
+// Both products are outer-product register tiles: a thread owns MR rows x 4
+// columns (per output), and per step of 4 along the contraction it loads
+// MR x 4 of the left operand (rows of E / O, or of A: one 16-byte load per
+// row) and 4 x 4 of the right operand (rows of the B slab, or of T), then
+// issues 16 MR FMAs per output.  A warp is RT x CT threads: a 32-column slab
+// takes CT = 8 column quads (8 rows per warp), a 16-column one CT = 4 (16
+// rows per warp), both with MR = 2.  Rows are interleaved (row = base + rt +
+// RT i), so the RT rows of one left-operand load are consecutive and fall in
+// distinct bank groups, and the CT column quads of a right-operand load are
+// one contiguous 128 (64) byte line.
+// MODE 0: acc0 = L0 R0; 1: also acc1 = L1 R0 (two left operands); 2: also
+// acc1 = L0 R1 (two right operands).  A thread owns MR rows x 4 columns.  Rows < nrows; the contraction runs over
+// K (a multiple of 4; the operands read as zero past their extent).  Results
+// go to shared memory (W row pitch wp) or, scaled, to global memory at
+// W + woff + row wp + column for columns < wcols.
+template <typename T, int CT, int MR, int MODE, bool GLOBAL>
+__device__ __forceinline__ void face2d_tiles(int nrows, int K, const T* L0, const T* L1, int lp, const T* R0,
+                                             const T* R1, int rp, T* W0, T* W1, long long wp, long long woff,
+                                             int wcols, T scale) {
+  constexpr int RT = 32 / CT;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ct = lane % CT, rt = lane / CT;
+  const int c0 = 4 * ct;
+  for (int rb = warp * MR * RT; rb < nrows; rb += kFace2DWarps * MR * RT) {
+    int row[MR];
+#pragma unroll
+    for (int i = 0; i < MR; ++i) row[i] = min(rb + rt + RT * i, nrows - 1);
+    T acc0[MR][4], acc1[MR][4];
+#pragma unroll
+    for (int i = 0; i < MR; ++i)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) { acc0[i][c] = 0; acc1[i][c] = 0; }
+#pragma unroll 2
+    for (int k = 0; k < K; k += 4) {
+      T r0[4][4], r1[4][4], l0[MR][4], l1[MR][4];
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        load4(R0 + (k + kk) * rp + c0, r0[kk]);
+        if constexpr (MODE == 2) load4(R1 + (k + kk) * rp + c0, r1[kk]);
+      }
+#pragma unroll
+      for (int i = 0; i < MR; ++i) {
+        load4(L0 + row[i] * lp + k, l0[i]);
+        if constexpr (MODE == 1) load4(L1 + row[i] * lp + k, l1[i]);
+      }
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+        for (int i = 0; i < MR; ++i)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            acc0[i][c] += l0[i][kk] * r0[kk][c];
+            if constexpr (MODE == 1) acc1[i][c] += l1[i][kk] * r0[kk][c];
+            if constexpr (MODE == 2) acc1[i][c] += l0[i][kk] * r1[kk][c];
+          }
+    }
+#pragma unroll
+    for (int i = 0; i < MR; ++i) {
+      const int r = rb + rt + RT * i;
+      if (r >= nrows) continue;
+      if constexpr (!GLOBAL) {
+        store4(W0 + r * wp + c0, acc0[i]);
+        if constexpr (MODE != 0) store4(W1 + r * wp + c0, acc1[i]);
+      } else {
+        T* p0 = W0 + woff + r * wp + c0;
+        T* p1 = (MODE != 0) ? W1 + woff + r * wp + c0 : nullptr;
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          if (c0 + c < wcols) {
+            p0[c] = acc0[i][c] * scale;
+            if constexpr (MODE != 0) p1[c] = acc1[i][c] * scale;
+          }
+      }
+    }
+  }
+}
+
+// Cluster item i is the job pair (jobs[2 i], jobs[2 i + 1]), CTA h taking
+// jobs[2 i + h].  Two whole jobs: each CTA runs its own.  A row-split job
+// (both entries the same): CTA h stages, combines and transforms rows
+// [r0, r0 + nr) of the layers (h = 0 the first ceil(V / 2)), writes its rows
+// of T, takes the other rows of T from its peer's shared memory (distributed
+// shared memory, between two cluster barriers) and writes rows [r0, r0 + nr)
+// of the outputs from its rows of A.  Both CTAs pass the two cluster
+// barriers of every item.
+//
+// CLUSTER false (a launch without split jobs): one CTA per job entry,
+// entries [0, 2 nitems), no cluster barriers.
+template <typename T, bool CLUSTER>
+__device__ __forceinline__ void face2d_body(T* __restrict__ buf, const Face2DJob* __restrict__ jobs, int nitems,
+                                            const Face2DSmem& sm) {
   grid_dependency_wait();
+  namespace cg = cooperative_groups;
+  const int half = CLUSTER ? (int)cg::this_cluster().block_rank() : 0;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* X0 = reinterpret_cast<T*>(smem_raw);
   T* X1 = X0 + sm.xs;
   T* Bs = X1 + sm.x1;
   T* T0 = Bs + sm.bs;
   T* T1 = T0 + sm.ts;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // warps in groups of 8: a group covers 32 consecutive rows (4 per warp, stride 8)
-  constexpr int kRowStep = 32 * (kFace2DThreads / 256);
-  const int wrow = (warp & 7) + 32 * (warp >> 3);
-  for (int jb = blockIdx.x; jb < njobs; jb += gridDim.x) {
-    const Face2DJob J = jobs[jb];
-    const int V = J.V, U = J.U;
-    const int Up = (U + 3) & ~3;
-    const int xp = Up + 4;
-    const int ap = ((V + 3) & ~3) + 4;
-    __syncthreads();  // previous job done with shared memory
-    // ---- stage X0, X1 and the B slab (asynchronous) ----
-    const T* g0 = buf + J.in0;
-    const T* g1 = buf + J.in1;
-    if (((U | J.ld) & 3) == 0 && ((J.in0 | J.in1) & 3) == 0) {
-      const int q4 = U >> 2;
-      for (int q = tid; q < V * q4; q += kFace2DThreads) {
-        const int r = q / q4, c = (q - r * q4) * 4;
-        const long long off = (long long)r * J.ld + c;
-        cp_async4(X0 + r * xp + c, g0 + off, true);
-        cp_async4(X1 + r * xp + c, g1 + off, true);
-      }
-    } else {
-      for (int i = tid; i < V * U; i += kFace2DThreads) {
-        const int r = i / U, c = i - r * U;
-        const long long off = (long long)r * J.ld + c;
-        cp_async_scalar(X0 + r * xp + c, g0 + off, true);
-        cp_async_scalar(X1 + r * xp + c, g1 + off, true);
-      }
-      for (int i = tid; i < V * (Up - U); i += kFace2DThreads) {  // columns U .. Up-1 read as zero
-        const int r = i / (Up - U), c = U + i - r * (Up - U);
-        X0[r * xp + c] = (T)0;
-        X1[r * xp + c] = (T)0;
-      }
-    }
-    const T* B = buf + J.tabB;
-    const int pb = face2d_pitch(U), pt = face2d_pitch(V);
-    for (int i = tid; i < Up * 32; i += kFace2DThreads) {
-      const int j = i >> 5, c = i & 31;
-      const bool ok = j < U && c < J.ub;
-      cp_async_scalar(Bs + c * pb + j, B + (ok ? (long long)j * U + J.u0 + c : 0), ok);
-    }
-    cp_async_commit();
-    cp_async_wait<0>();
-    __syncthreads();
-    for (int i = tid; i < V * xp; i += kFace2DThreads) {
-      const T a = X0[i], b = X1[i];
-      X0[i] = a + b;
-      X1[i] = a - b;
-    }
-    __syncthreads();
-    // ---- along U: T0 = E B, T1 = O B (lane = column, warp = row group) ----
-    // narrow jobs (16 columns): lanes 0-15 and 16-31 take the same columns on
-    // interleaved rows, so the warp stays fully busy
-    const int col = J.narrow ? (lane & 15) : lane;
-    const int rsub = J.narrow ? 8 * (lane >> 4) : 0;
-    const int rstr = J.narrow ? 16 : 8;
-    const int rstep = J.narrow ? 2 * kRowStep : kRowStep;
-    const int wrow0 = J.narrow ? (warp & 7) + 64 * (warp >> 3) : wrow;
-    auto along_u = [&](auto de, auto dodd) {
-      constexpr bool DE = decltype(de)::value, DO = decltype(dodd)::value;
-      for (int r0 = wrow0 + rsub; r0 - rsub < V; r0 += rstep) {
-        T e[4] = {0, 0, 0, 0}, o[4] = {0, 0, 0, 0};
-        int rr[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) rr[i] = min(r0 + rstr * i, V - 1);
-        for (int j = 0; j < U; j += 4) {
-          T bq[4];
-          load4(Bs + col * pb + j, bq);
-          const T b0 = bq[0], b1 = bq[1], b2 = bq[2], b3 = bq[3];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            T x[4], y[4];
-            if constexpr (DE) {
-              load4(X0 + rr[i] * xp + j, x);
-              e[i] += x[0] * b0 + x[1] * b1 + x[2] * b2 + x[3] * b3;
-            }
-            if constexpr (DO) {
-              load4(X1 + rr[i] * xp + j, y);
-              o[i] += y[0] * b0 + y[1] * b1 + y[2] * b2 + y[3] * b3;
-            }
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-          if (r0 + rstr * i < V) {
-            if constexpr (DE) T0[col * pt + r0 + rstr * i] = e[i];
-            if constexpr (DO) T1[col * pt + r0 + rstr * i] = o[i];
-          }
-      }
-    };
-    if (J.which == 0) along_u(std::true_type{}, std::true_type{});
-    else if (J.which == 1) along_u(std::true_type{}, std::false_type{});
-    else along_u(std::false_type{}, std::true_type{});
-    {  // rows V .. roundup(V, 4) - 1 of T read as zero
-      const int vt = ((V + 3) & ~3) - V;
-      for (int i = tid; i < 32 * vt; i += kFace2DThreads) {
-        const int c = i / vt, r = V + i - c * vt;
-        T0[c * pt + r] = (T)0;
-        T1[c * pt + r] = (T)0;
-      }
-    }
-    __syncthreads();
-    // ---- A (V x V, row o contiguous) into the X0 area (asynchronous) ----
-    const T* A = buf + J.tabA;
-    if ((V & 3) == 0 && (J.tabA & 3) == 0) {
-      const int a4 = ap >> 2;
-      for (int q = tid; q < V * a4; q += kFace2DThreads) {
-        const int o = q / a4, r = (q - o * a4) * 4;
-        const bool ok = r < V;
-        cp_async4(X0 + o * ap + r, A + (ok ? (long long)o * V + r : 0), ok);
-      }
-    } else {
-      for (int i = tid; i < V * ap; i += kFace2DThreads) {
-        const int o = i / ap, r = i - o * ap;
-        const bool ok = r < V;
-        cp_async_scalar(X0 + i, A + (ok ? (long long)o * V + r : 0), ok);
-      }
-    }
-    cp_async_commit();
-    cp_async_wait<0>();
-    __syncthreads();
-    // ---- along V: out = scale A T ----
-    const T scale = (T)J.scale;
-    auto along_v = [&](auto de, auto dodd) {
-      constexpr bool DE = decltype(de)::value, DO = decltype(dodd)::value;
-      for (int o0 = wrow0 + rsub; o0 - rsub < V; o0 += rstep) {
-        T e[4] = {0, 0, 0, 0}, od[4] = {0, 0, 0, 0};
-        int oo[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) oo[i] = min(o0 + rstr * i, V - 1);
-        for (int r = 0; r < V; r += 4) {
-          T t[4], u[4];
-          if constexpr (DE) load4(T0 + col * pt + r, t);
-          if constexpr (DO) load4(T1 + col * pt + r, u);
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            T a4[4];
-            load4(X0 + oo[i] * ap + r, a4);
-            if constexpr (DE) e[i] += a4[0] * t[0] + a4[1] * t[1] + a4[2] * t[2] + a4[3] * t[3];
-            if constexpr (DO) od[i] += a4[0] * u[0] + a4[1] * u[1] + a4[2] * u[2] + a4[3] * u[3];
-          }
-        }
-        if (col < J.ub) {
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-            if (o0 + rstr * i < V) {
-              const long long off = (long long)(o0 + rstr * i) * J.ld + J.u0 + col;
-              if constexpr (DE) buf[J.out0 + off] = e[i] * scale;
-              if constexpr (DO) buf[J.out1 + off] = od[i] * scale;
-            }
-        }
-      }
-    };
-    if (J.which == 0) along_v(std::true_type{}, std::true_type{});
-    else if (J.which == 1) along_v(std::true_type{}, std::false_type{});
-    else along_v(std::false_type{}, std::true_type{});
+  const T* P0 = T0;   // the peer's T (cluster launches)
+  const T* P1 = T1;
+  if constexpr (CLUSTER) {
+    P0 = cg::this_cluster().map_shared_rank(T0, half ^ 1);
+    P1 = cg::this_cluster().map_shared_rank(T1, half ^ 1);
   }
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int first = CLUSTER ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+  const int stride = CLUSTER ? (int)(gridDim.x >> 1) : (int)gridDim.x;
+  const int count = CLUSTER ? nitems : 2 * nitems;
+  for (int it = first; it < count; it += stride) {
+    const Face2DJob J = jobs[CLUSTER ? 2 * it + half : it];
+    const int V = J.V, U = J.U;
+    const int Up = (U + 3) & ~3, Vp = (V + 3) & ~3;
+    const int xp = face2d_pitch(U), ap = face2d_pitch(V);
+    const int cq = J.narrow ? 4 : 8;    // column quads of the slab
+    const int bp = 4 * cq;              // row pitch of the B slab and of T
+    const int nh = (V + 1) >> 1;        // rows of the first half of a split job
+    const int r0 = (J.split && half) ? nh : 0;                 // this CTA's rows
+    const int nr = J.split ? (half ? V - nh : nh) : V;
+    const int p0 = half ? 0 : nh;                              // the peer's rows (split jobs)
+    const int pn = J.split ? (half ? nh : V - nh) : 0;
+    __syncthreads();  // previous job done with shared memory
+    // ---- stage rows r0 .. r0 + nr - 1 of X0, X1 (columns U .. Up-1 zero)
+    // and the B slab (asynchronous) ----
+    const T* g0 = buf + J.in0 + (long long)r0 * J.ld;
+    const T* g1 = buf + J.in1 + (long long)r0 * J.ld;
+    const int q4 = Up >> 2;
+    const bool xvec = ((U | J.ld) & 3) == 0 && ((J.in0 | J.in1) & 3) == 0;
+    for (int r = warp; r < nr; r += kFace2DWarps)
+      for (int q = lane; q < q4; q += 32) {
+        const int c = 4 * q;
+        const long long off = (long long)r * J.ld + c;
+        if (xvec) {
+          cp_async4(X0 + r * xp + c, g0 + off, true);
+          cp_async4(X1 + r * xp + c, g1 + off, true);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const bool ok = c + e < U;
+            cp_async_scalar(X0 + r * xp + c + e, g0 + (ok ? off + e : 0), ok);
+            cp_async_scalar(X1 + r * xp + c + e, g1 + (ok ? off + e : 0), ok);
+          }
+        }
+      }
+    const T* B = buf + J.tabB;
+    const bool bvec = ((U | J.u0) & 3) == 0 && (J.tabB & 3) == 0;
+    for (int i = tid; i < Up * cq; i += kFace2DThreads) {
+      const int j = i / cq, c = 4 * (i - j * cq);
+      const long long off = (long long)j * U + J.u0 + c;
+      if (bvec && j < U && c + 3 < J.ub) {
+        cp_async4(Bs + j * bp + c, B + off, true);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const bool ok = j < U && c + e < J.ub;
+          cp_async_scalar(Bs + j * bp + c + e, B + (ok ? off + e : 0), ok);
+        }
+      }
+    }
+    cp_async_commit();
+    // rows V .. Vp-1 of T read as zero in the second product
+    for (int i = tid; i < (Vp - V) * bp; i += kFace2DThreads) {
+      T0[V * bp + i] = (T)0;
+      T1[V * bp + i] = (T)0;
+    }
+    cp_async_wait<0>();
+    __syncthreads();
+    // ---- E = X0 + X1, O = X0 - X1 (a one-output job keeps its part in X0) ----
+    for (int r = warp; r < nr; r += kFace2DWarps)
+      for (int q = lane; q < q4; q += 32) {
+        T a[4], b[4], e[4], o[4];
+        load4(X0 + r * xp + 4 * q, a);
+        load4(X1 + r * xp + 4 * q, b);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { e[k] = a[k] + b[k]; o[k] = a[k] - b[k]; }
+        if (J.which == 2) {
+          store4(X0 + r * xp + 4 * q, o);
+        } else {
+          store4(X0 + r * xp + 4 * q, e);
+          if (J.which == 0) store4(X1 + r * xp + 4 * q, o);
+        }
+      }
+    __syncthreads();
+    // ---- rows r0 .. r0 + nr - 1 of A (V x V, columns V .. Vp-1 zero) into
+    // X1 (one output, overlapping the first product) or into X0 after it ----
+    const T* A = buf + J.tabA + (long long)r0 * V;
+    const bool avec = (V & 3) == 0 && (J.tabA & 3) == 0;
+    auto stage_a = [&](T* dst) {
+      const int a4 = Vp >> 2;
+      for (int o = warp; o < nr; o += kFace2DWarps)
+        for (int q = lane; q < a4; q += 32) {
+          const int r = 4 * q;
+          const long long off = (long long)o * V + r;
+          if (avec) {
+            cp_async4(dst + o * ap + r, A + off, true);
+          } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const bool ok = r + e < V;
+              cp_async_scalar(dst + o * ap + r + e, A + (ok ? off + e : 0), ok);
+            }
+          }
+        }
+      cp_async_commit();
+    };
+    const bool one = J.which != 0;
+    if (one) stage_a(X1);
+    // ---- along U: rows r0 .. of T0 (, T1) = E (, O) B over the slab ----
+    T* W0 = T0 + r0 * bp;
+    T* W1 = T1 + r0 * bp;
+    if (J.narrow) {
+      if (one) face2d_tiles<T, 4, 2, 0, false>(nr, Up, X0, X0, xp, Bs, Bs, bp, W0, W0, bp, 0, 0, (T)1);
+      else     face2d_tiles<T, 4, 2, 1, false>(nr, Up, X0, X1, xp, Bs, Bs, bp, W0, W1, bp, 0, 0, (T)1);
+    } else {
+      if (one) face2d_tiles<T, 8, 2, 0, false>(nr, Up, X0, X0, xp, Bs, Bs, bp, W0, W0, bp, 0, 0, (T)1);
+      else     face2d_tiles<T, 8, 2, 1, false>(nr, Up, X0, X1, xp, Bs, Bs, bp, W0, W1, bp, 0, 0, (T)1);
+    }
+    if constexpr (CLUSTER) cg::this_cluster().sync();   // both halves of T written; E and O consumed
+    else __syncthreads();
+    if (!one) stage_a(X0);
+    // the peer's rows of T
+    for (int i = tid; i < pn * cq; i += kFace2DThreads) {
+      const int r = p0 + i / cq, c = 4 * (i % cq);
+      T v[4];
+      load4(P0 + r * bp + c, v);
+      store4(T0 + r * bp + c, v);
+      if (!one) {
+        load4(P1 + r * bp + c, v);
+        store4(T1 + r * bp + c, v);
+      }
+    }
+    cp_async_wait<0>();
+    if constexpr (CLUSTER) cg::this_cluster().sync();   // copies done (the peer may reuse its T); A staged
+    else __syncthreads();
+    // ---- along V: rows r0 .. of out = scale A T ----
+    const T* As = one ? X1 : X0;
+    T* o0 = (J.which == 2) ? buf + J.out1 : buf + J.out0;
+    T* o1 = (J.which == 0) ? buf + J.out1 : nullptr;
+    const long long w0 = J.u0 + (long long)r0 * J.ld;
+    const T sc = (T)J.scale;
+    if (J.narrow) {
+      if (one) face2d_tiles<T, 4, 2, 0, true>(nr, Vp, As, As, ap, T0, T0, bp, o0, o0, J.ld, w0, J.ub, sc);
+      else     face2d_tiles<T, 4, 2, 2, true>(nr, Vp, As, As, ap, T0, T1, bp, o0, o1, J.ld, w0, J.ub, sc);
+    } else {
+      if (one) face2d_tiles<T, 8, 2, 0, true>(nr, Vp, As, As, ap, T0, T0, bp, o0, o0, J.ld, w0, J.ub, sc);
+      else     face2d_tiles<T, 8, 2, 2, true>(nr, Vp, As, As, ap, T0, T1, bp, o0, o1, J.ld, w0, J.ub, sc);
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kFace2DThreads, 2) face2d_kernel(T* __restrict__ buf, const Face2DJob* __restrict__ jobs,
+                                                                  int nitems, Face2DSmem sm) {
+  face2d_body<T, false>(buf, jobs, nitems, sm);
+}
+
+template <typename T>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kFace2DThreads, 2)
+    face2d_cluster_kernel(T* __restrict__ buf, const Face2DJob* __restrict__ jobs, int nitems, Face2DSmem sm) {
+  face2d_body<T, true>(buf, jobs, nitems, sm);
+}
+
+// Launch of the face transforms over n cluster items (2 n job entries):
+// clusters of two CTAs where the list holds row-split jobs, else one CTA per
+// entry; at most max_ctas CTAs.
+template <typename T>
+inline cudaError_t launch_face2d(bool split, long long n, int max_ctas, size_t smem, cudaStream_t s, T* buf,
+                                 const Face2DJob* jobs, const Face2DSmem& sm) {
+  if (n <= 0) return cudaSuccess;
+  if (split) {
+    const long long c = std::max(1LL, std::min(n, (long long)(max_ctas / 2)));
+    return launch_dep(face2d_cluster_kernel<T>, 2 * c, kFace2DThreads, smem, s, buf, jobs, (int)n, sm);
+  }
+  const long long b = std::max(1LL, std::min(2 * n, (long long)max_ctas));
+  return launch_dep(face2d_kernel<T>, b, kFace2DThreads, smem, s, buf, jobs, (int)n, sm);
 }
 
 // ---------------------------------------------------------------------------

@@ -137,37 +137,80 @@ int zero_state(Ctx* ctx) {
   return ARD_OK;
 }
 
-// Splits the largest two-output face jobs into one-output jobs (the same
-// staging, half the arithmetic) while the list still fits in one wave of
-// `slots` blocks: the launch lasts as long as its largest job.  Largest
-// first afterwards.
-void balance_face_jobs(std::vector<Face2DJob>* jobs, int slots) {
-  // arithmetic of a job: both transforms over its columns, for one or two outputs
+// Balances the face jobs of one launch and pairs them for the two CTAs of a
+// cluster.  While the launch still fits in one wave of `slots` CTAs (it then
+// lasts as long as its largest job), the largest job is split: a two-output
+// job into one job per output (the same staging, half the arithmetic), then
+// a one-output job's rows between the two CTAs of its cluster (half the
+// staging and arithmetic each, the halves of T exchanged through distributed
+// shared memory).  A launch of many waves keeps whole jobs, two to a cluster,
+// one per CTA.  A 16-column job costs its warps as much as a 32-column one
+// (16 rows per warp instead of 8), so column splits would not shorten the
+// launch and are not made.  Output: pairs (jobs[2 i], jobs[2 i + 1]) for the
+// cluster of item i, largest first: a split job twice, or two whole jobs (the
+// last one padded by an empty job).  Returns whether any job's rows are split
+// (the launch then runs in clusters; without, one CTA per entry).
+bool balance_face_jobs(std::vector<Face2DJob>* jobs, int slots) {
+  // the arithmetic of one warp of a CTA of the job: rows of the warp's row
+  // blocks x the slab's columns x both contractions, for one or two outputs
   auto work = [](const Face2DJob& j) {
-    return (long long)j.V * (j.U + j.V) * (j.which == 0 ? 2 : 1) * (j.narrow ? 16 : 32);
+    const int rows = j.narrow ? 16 : 8, per_block = rows * kFace2DWarps;
+    const int nr = j.split ? (j.V + 1) / 2 : j.V;
+    return (long long)((nr + per_block - 1) / per_block) * rows * (j.narrow ? 16 : 32) * (j.U + j.V) *
+           (j.which == 0 ? 2 : 1);
   };
-  for (Face2DJob& j : *jobs) j.narrow = j.ub <= 16 ? 1 : 0;
-  while ((int)jobs->size() < slots && !jobs->empty()) {
+  for (Face2DJob& j : *jobs) {
+    j.narrow = j.ub <= 16 ? 1 : 0;
+    j.split = 0;
+  }
+  long long ctas = (long long)jobs->size();
+  while (ctas < slots && !jobs->empty()) {
     size_t k = 0;
     for (size_t i = 1; i < jobs->size(); ++i)
       if (work((*jobs)[i]) > work((*jobs)[k])) k = i;
     Face2DJob& J = (*jobs)[k];
-    if (J.which == 0) {            // one block per output
+    if (J.which == 0) {            // one job per output
       Face2DJob b = J;
       J.which = 1;
       b.which = 2;
       jobs->push_back(b);
-    } else if (!J.narrow) {        // two 16-column halves
-      Face2DJob b = J;
-      J.ub = 16; J.narrow = 1;
-      b.u0 += 16; b.ub -= 16; b.narrow = 1;
-      jobs->push_back(b);
+      ctas += 1;
+    } else if (!J.split && J.V > 1) {   // rows split over the cluster
+      J.split = 1;
+      ctas += 1;
     } else {
       break;                       // the largest job cannot be split further
     }
   }
   std::stable_sort(jobs->begin(), jobs->end(),
                    [&](const Face2DJob& a, const Face2DJob& b) { return work(a) > work(b); });
+  bool split = false;
+  for (const Face2DJob& J : *jobs) split = split || J.split;
+  std::vector<Face2DJob> out;
+  out.reserve(2 * jobs->size() + 2);
+  bool pending = false;
+  Face2DJob wait{};
+  for (const Face2DJob& J : *jobs) {
+    if (J.split) {
+      out.push_back(J);
+      out.push_back(J);
+    } else if (pending) {
+      out.push_back(wait);
+      out.push_back(J);
+      pending = false;
+    } else {
+      wait = J;
+      pending = true;
+    }
+  }
+  if (pending) {
+    Face2DJob idle{};              // V = 0: no rows, no stores
+    idle.which = 1;
+    out.push_back(wait);
+    out.push_back(idle);
+  }
+  *jobs = std::move(out);
+  return split;
 }
 
 // Face transforms of the adjoint step, the transposes of the forward ones:
@@ -825,11 +868,11 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
       for (const Ax& a : axes) {
         const long long LS = (long long)a.V * a.ld;
         const long long UU = (long long)a.U * a.U, VV = (long long)a.V * a.V;
-        const long long xp = ((a.U + 3) & ~3) + 4, ap = ((a.V + 3) & ~3) + 4;
-        xs = std::max(xs, std::max((long long)a.V * xp, (long long)a.V * ap));
-        x1 = std::max(x1, (long long)a.V * xp);
-        bs = std::max(bs, 32LL * face2d_pitch(a.U));
-        ts = std::max(ts, 32LL * face2d_pitch(a.V));
+        const long long xp = face2d_pitch(a.U), ap = face2d_pitch(a.V);
+        xs = std::max(xs, (long long)a.V * std::max(xp, ap));   // whole jobs (the eligibility of the fused form)
+        x1 = xs;
+        bs = std::max(bs, 32LL * ((a.U + 3) & ~3));
+        ts = std::max(ts, 32LL * ((a.V + 3) & ~3));
         for (int u0 = 0; u0 < a.U; u0 += 32) {
           const int ub = std::min(32, a.U - u0);
           for (int n = 0; n < 3; ++n) {
@@ -910,13 +953,14 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
     }
   }
   if (ctx->fused_faces) {
-    const int per_sm = std::max(1, (int)(ctx->smem_per_sm / (ctx->f2d_bytes + 1024)));
-    const int slots = ctx->num_sms * per_sm;
+    // CTAs of one wave: two per SM (the kernel's bound; the shared memory of
+    // row-split jobs, sized below, is about half that of whole ones)
+    const int slots = ctx->num_sms * 2;
     // each group gets a share of one wave in proportion to its arithmetic
     auto grouped = [&](std::vector<Face2DJob>* list, auto set_range) {
       if (ctx->ngroups == 1) {
-        balance_face_jobs(list, slots);
-        set_range(0, 0, (int)list->size());
+        const bool sp = balance_face_jobs(list, slots);
+        set_range(0, 0, (int)list->size() / 2, sp);
         return;
       }
       std::vector<Face2DJob> parts[2];
@@ -929,16 +973,34 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
       list->clear();
       for (int g = 0; g < 2; ++g) {
         const int sg = std::max(1, (int)std::lround(slots * w[g] / std::max(1.0, w[0] + w[1])));
-        balance_face_jobs(&parts[g], sg);
-        const int lo = (int)list->size();
+        const bool sp = balance_face_jobs(&parts[g], sg);
+        const int lo = (int)list->size() / 2;
         list->insert(list->end(), parts[g].begin(), parts[g].end());
-        set_range(g, lo, (int)list->size());
+        set_range(g, lo, (int)list->size() / 2, sp);
       }
     };
-    grouped(&ctx->fwd2d, [&](int g, int lo, int hi) { ctx->groups[g].f_lo = lo; ctx->groups[g].f_hi = hi; });
-    grouped(&ctx->inv2d, [&](int g, int lo, int hi) { ctx->groups[g].i_lo = lo; ctx->groups[g].i_hi = hi; });
-    balance_face_jobs(&ctx->adj1_2d, slots);
-    balance_face_jobs(&ctx->adj2_2d, slots);
+    grouped(&ctx->fwd2d, [&](int g, int lo, int hi, bool sp) {
+      ctx->groups[g].f_lo = lo; ctx->groups[g].f_hi = hi; ctx->groups[g].f_split = sp;
+    });
+    grouped(&ctx->inv2d, [&](int g, int lo, int hi, bool sp) {
+      ctx->groups[g].i_lo = lo; ctx->groups[g].i_hi = hi; ctx->groups[g].i_split = sp;
+    });
+    ctx->adj1_split = balance_face_jobs(&ctx->adj1_2d, slots);
+    ctx->adj2_split = balance_face_jobs(&ctx->adj2_2d, slots);
+    // shared memory of the balanced jobs: a CTA stages its rows of the layers
+    // (all V, or half of a split job) and all of T
+    const size_t es0 = elem_size(ctx);
+    long long xs = 0, bs = 0, ts = 0;
+    for (const std::vector<Face2DJob>* L : {&ctx->fwd2d, &ctx->inv2d, &ctx->adj1_2d, &ctx->adj2_2d})
+      for (const Face2DJob& j : *L) {
+        if (j.V == 0) continue;
+        const long long rows = j.split ? (j.V + 1) / 2 : j.V;
+        xs = std::max(xs, rows * std::max(face2d_pitch(j.U), face2d_pitch(j.V)));
+        bs = std::max(bs, 32LL * ((j.U + 3) & ~3));
+        ts = std::max(ts, 32LL * ((j.V + 3) & ~3));
+      }
+    ctx->f2d_smem = Face2DSmem{(int)xs, (int)xs, (int)bs, (int)ts};
+    ctx->f2d_bytes = (size_t)(2 * xs + bs + 2 * ts) * es0;
   }
 
   // ---- device allocation ----

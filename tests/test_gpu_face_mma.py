@@ -54,9 +54,12 @@ def test_tensor_core_faces_match_reference(name, monkeypatch):
             continue
         assert rel_l2(got[:, r], want[:, r]) < F32_TOL, (name, r)
         assert rel_l2(got[:, r], base[:, r]) < 1e-5, (name, r)
-    for part in range(len(sc["air"])):
-        a, b = mma.field(part), fused.field(part)
-        assert np.abs(a - b).max() <= 1e-5 * max(np.abs(b).max(), 1e-30), part
+    # fields against the scene's largest value: a quiet partition's FP32
+    # rounding is set by the loudest field that reaches it through the interfaces
+    fields = [(mma.field(part), fused.field(part)) for part in range(len(sc["air"]))]
+    scale = max(max(np.abs(b).max() for _, b in fields), 1e-30)
+    for part, (a, b) in enumerate(fields):
+        assert np.abs(a - b).max() <= 1e-5 * scale, part
 
 
 def test_tensor_core_faces_ragged_two_partitions(monkeypatch):
