@@ -44,6 +44,9 @@ advanced one time step; PML cells are extra work, not counted.
           is the recorder signal of the timed forward run; face scales
           U(0.5, 1.5), seeded): wall time of the ard_adjoint call against the
           device time of the forward steps
+  batched_vs_plain  the first 16 scenes of the batched workload (c2) for 320
+          steps in one context against one context per scene run one after
+          another, host wall clock
   cpu_baseline  the oracle (C restatement of the reference's CPU solver,
           FP32, OpenMP over partitions) on a bounded sample of the same scene
   --plain runs every scene in its own context one after another (the
@@ -395,6 +398,44 @@ def adjoint_measurement(A, cfg, scenes, args, device, series, target, fwd_s_per_
     return out
 
 
+def batching_measurement(A, device, n_scenes=16, T=320):
+    """Batched against plain on the batched workload's scenes: the first
+    `n_scenes` c2 scenes for T steps, in one context (one launch per stage
+    over all scenes, the production path) and in one context per scene run
+    one after another (the per-scene path), each after 64 warm-up steps and
+    a reset; host wall clock around the runs and a synchronize after each."""
+    cfg = workload("c2", T)
+    cfg = dict(cfg, scenes=cfg["scenes"][:n_scenes])
+    h32 = float(np.float32(cfg["h"]))
+    scenes = [A.build_scene(sc["air"], sc["sources"], sc["recorders"], h32, cfg["dt"], cfg["c0"], cfg["pml"])
+              for sc in cfg["scenes"]]
+    n_air = sum(s.air_cells for s in scenes)
+
+    def timed(groups):
+        sims = []
+        for g in groups:
+            sim = A.Simulation([scenes[i] for i in g], max_steps=T, device=device)
+            load_series(sim, dict(cfg, scenes=[cfg["scenes"][i] for i in g]), T)
+            sim.run(64)
+            sim.synchronize()
+            sim.reset()
+            sims.append(sim)
+        t0 = time.perf_counter()
+        for sim in sims:
+            sim.run(T)
+            sim.synchronize()
+        dt = time.perf_counter() - t0
+        for sim in sims:
+            sim.close()
+        return n_air * T / dt / 1e9
+
+    batched = timed([list(range(len(scenes)))])
+    plain = timed([[i] for i in range(len(scenes))])
+    return {"workload": f"c2: first {len(scenes)} scenes, {n_air} air cells, {T} steps",
+            "batched": batched, "plain": plain, "unit": UNIT, "ratio": batched / plain,
+            "timing": "host wall clock around the runs (synchronize after each context's run)"}
+
+
 def profile_run(args):
     """N direct-launch steps of the workload (its first --profile-scenes
     scenes), so that every kernel is a separate launch for ncu; prints the
@@ -434,6 +475,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-reference-arithmetic", action="store_true")
+    ap.add_argument("--no-batching", action="store_true", help="skip the batched-against-plain measurement")
     ap.add_argument("--adjoint-steps", type=int, default=None,
                     help="steps of the adjoint measurement (default: the whole simulation)")
     ap.add_argument("--checkpoint-every", type=int, default=0,
@@ -686,6 +728,8 @@ def main():
         if args.steps * chunk >= Sa or Sa <= chunk:
             line["adjoint"] = adjoint_measurement(A, cfg, scenes, args, local, series, recorded[:Sa].copy(),
                                                   fwd_s_per_time_step)
+    if not args.no_batching and not args.plain and rank == 0:
+        line["batched_vs_plain"] = batching_measurement(A, local)
     if rank == 0 and not args.no_cpu_baseline:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
         line["cpu_baseline"] = cpu_baseline(cfg, args.cpu_sample, args.cpu_seconds)
