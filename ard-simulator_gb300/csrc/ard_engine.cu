@@ -459,7 +459,7 @@ int launch_post_modal_range(Ctx* ctx, cudaStream_t s, int tstep, int r_lo, int r
                             long long s_first, long long s_total) {
   const int nrec = r_hi - r_lo;
   const int rec_blocks = (nrec * 32 + 255) / 256;
-  const int sum_blocks = s_total > 0 ? grid_for(s_total, 256, ctx->num_sms * 8) : 0;
+  const int sum_blocks = s_total > 0 ? grid_for(s_total, kSumChunk, ctx->num_sms * 8) : 0;
   if (rec_blocks + sum_blocks == 0) return ARD_OK;
   PostModalArgs<T> a{reinterpret_cast<T*>(ctx->d_buf), ctx->d_dct, ctx->d_recpts, r_lo, nrec, ctx->n_rec_total,
                      ctx->d_hist, ctx->d_t, tstep, ctx->max_steps, rec_blocks, ctx->d_psum + s_lo, s_hi - s_lo,

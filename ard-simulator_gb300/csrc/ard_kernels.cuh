@@ -522,7 +522,10 @@ inline cudaError_t configure_face_gemm() {
 // ---------------------------------------------------------------------------
 
 // In-place sum of the per-tile partial slabs of the modal contraction:
-// slab 0 of each job receives the sum of its nb slabs (fixed order).
+// slab 0 of each job receives the sum of its nb slabs (fixed order).  A
+// job's elements occupy [first, first + count) of the launch's index space,
+// first a multiple of kSumChunk.
+constexpr int kSumChunk = 2048;
 struct SumJob {
   long long base;     // slab 0
   long long count;    // elements per slab
@@ -534,7 +537,8 @@ struct SumJob {
 // After the modal update: the recorder samples of the step (blocks
 // [0, rec_blocks): one warp per recorder, the sum of the tiles' partials
 // times s_i into the double history) and the in-place partial sums (the
-// other blocks, grid-stride).  One launch for both.
+// other blocks, grid-stride over chunks of kSumChunk elements).  One launch
+// for both.
 template <typename T>
 struct PostModalArgs {
   T* buf;
@@ -573,34 +577,47 @@ __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
     return;
   }
   T* __restrict__ buf = a.buf;
-  // first elements of the jobs, cached for the per-element job search
+  // first elements of the jobs, cached for the per-chunk job search
   constexpr int kMaxCachedJobs = 1024;
   __shared__ long long sfirst[kMaxCachedJobs];
   const bool cached = a.njobs <= kMaxCachedJobs;
   if (cached)
     for (int i = threadIdx.x; i < a.njobs; i += blockDim.x) sfirst[i] = a.jobs[i].first;
   __syncthreads();
+  // chunks of kSumChunk elements: a job's elements start on a chunk boundary
+  // of the index space, so a chunk lies in one job; a thread sums 8 elements
+  // (256 apart) over the job's slabs, slab by slab in order
   const long long nb = (long long)gridDim.x - a.rec_blocks;
-  for (long long g = ((long long)blockIdx.x - a.rec_blocks) * blockDim.x + threadIdx.x; g < a.total;
-       g += nb * blockDim.x) {
-    const long long gg = g + a.first;   // element index among all sum jobs
+  const long long nchunks = a.total / kSumChunk;
+  for (long long ch = (long long)blockIdx.x - a.rec_blocks; ch < nchunks; ch += nb) {
+    const long long gg = a.first + ch * kSumChunk;   // first element of the chunk among all sum jobs
     int lo = 0, hi = a.njobs - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
       if ((cached ? sfirst[mid] : a.jobs[mid].first) <= gg) lo = mid; else hi = mid - 1;
     }
     const SumJob J = a.jobs[lo];
-    const T* p = buf + J.base + (gg - J.first);
-    T v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int b = 0;
-    for (; b + 8 <= J.nb; b += 8) {
+    const long long e0 = gg - J.first;
+    T* p = buf + J.base + e0;
+    constexpr int kPer = kSumChunk / 256;
+    bool ok[kPer];
+    T v[kPer];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) v[k] += p[(long long)(b + k) * J.stride];
+    for (int i = 0; i < kPer; ++i) {
+      const int idx = (int)threadIdx.x + 256 * i;
+      ok[i] = e0 + idx < J.count;
+      v[i] = ok[i] ? p[idx] : (T)0;
+    }
+#pragma unroll 2
+    for (int b = 1; b < J.nb; ++b) {
+      const T* q = p + (long long)b * J.stride;
+#pragma unroll
+      for (int i = 0; i < kPer; ++i)
+        if (ok[i]) v[i] += q[threadIdx.x + 256 * i];
     }
 #pragma unroll
-    for (int k = 0; k < 7; ++k)
-      if (b + k < J.nb) v[k] += p[(long long)(b + k) * J.stride];
-    buf[J.base + (gg - J.first)] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+    for (int i = 0; i < kPer; ++i)
+      if (ok[i]) p[threadIdx.x + 256 * i] = v[i];
   }
 }
 

@@ -804,7 +804,7 @@ int build_layout(Ctx* ctx, const ard_scene* scenes, int n_scenes) {
       if (nb[k] < 2) continue;
       SumJob j{base[k], cnt[k], cnt[k], ctx->psum_total, nb[k]};
       ctx->psum.push_back(j);
-      ctx->psum_total += cnt[k];
+      ctx->psum_total += (cnt[k] + kSumChunk - 1) / kSumChunk * kSumChunk;   // chunk-aligned index space
     }
   }
 
