@@ -459,11 +459,16 @@ int launch_post_modal_range(Ctx* ctx, cudaStream_t s, int tstep, int r_lo, int r
                             long long s_first, long long s_total) {
   const int nrec = r_hi - r_lo;
   const int rec_blocks = (nrec * 32 + 255) / 256;
-  const int sum_blocks = s_total > 0 ? grid_for(s_total, kSumChunk, ctx->num_sms * 8) : 0;
+  // chunks of 8 elements per thread where the chunks fill a wave of blocks;
+  // one element per thread for smaller launches
+  const int wave = ctx->num_sms * 8;
+  const long long nchunks = s_total / kSumChunk;
+  const int per = nchunks >= wave ? 8 : 0;
+  const int sum_blocks = s_total <= 0 ? 0 : (per ? grid_for(nchunks, 1, wave) : grid_for(s_total, 256, wave));
   if (rec_blocks + sum_blocks == 0) return ARD_OK;
   PostModalArgs<T> a{reinterpret_cast<T*>(ctx->d_buf), ctx->d_dct, ctx->d_recpts, r_lo, nrec, ctx->n_rec_total,
                      ctx->d_hist, ctx->d_t, tstep, ctx->max_steps, rec_blocks, ctx->d_psum + s_lo, s_hi - s_lo,
-                     s_first, s_total};
+                     s_first, s_total, per};
   ARD_CUDA(launch_dep(post_modal_kernel<T>, rec_blocks + sum_blocks, 256, 0, s, a));
   ARD_CUDA(cudaGetLastError());
   return ARD_OK;

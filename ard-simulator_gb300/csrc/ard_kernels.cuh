@@ -537,8 +537,9 @@ struct SumJob {
 // After the modal update: the recorder samples of the step (blocks
 // [0, rec_blocks): one warp per recorder, the sum of the tiles' partials
 // times s_i into the double history) and the in-place partial sums (the
-// other blocks, grid-stride over chunks of kSumChunk elements).  One launch
-// for both.
+// other blocks: launches of at least a wave of chunks grid-stride over
+// chunks of kSumChunk elements, 8 per thread; smaller ones take one element
+// per thread with all its slabs in flight).  One launch for both.
 template <typename T>
 struct PostModalArgs {
   T* buf;
@@ -554,7 +555,8 @@ struct PostModalArgs {
   const SumJob* jobs;     // this launch's sum jobs; their elements start at `first`
   int njobs;
   long long first;
-  long long total;
+  long long total;        // a multiple of kSumChunk
+  int per;                // elements per thread: 1, 2, 4 or 8 (chunked), 0: one element per thread
 };
 
 template <typename T>
@@ -588,8 +590,41 @@ __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
   // of the index space, so a chunk lies in one job; a thread sums 8 elements
   // (256 apart) over the job's slabs, slab by slab in order
   const long long nb = (long long)gridDim.x - a.rec_blocks;
-  const long long nchunks = a.total / kSumChunk;
-  for (long long ch = (long long)blockIdx.x - a.rec_blocks; ch < nchunks; ch += nb) {
+  if (a.per == 0) {
+    // small launches: one element per thread, all its slabs in flight at once
+    for (long long g = ((long long)blockIdx.x - a.rec_blocks) * blockDim.x + threadIdx.x; g < a.total;
+         g += nb * blockDim.x) {
+      const long long gg = g + a.first;
+      int lo = 0, hi = a.njobs - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((cached ? sfirst[mid] : a.jobs[mid].first) <= gg) lo = mid; else hi = mid - 1;
+      }
+      const SumJob J = a.jobs[lo];
+      const long long e = gg - J.first;
+      if (e >= J.count) continue;   // the chunk padding of the index space
+      const T* p = buf + J.base + e;
+      T v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      int b = 0;
+      for (; b + 8 <= J.nb; b += 8) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] += p[(long long)(b + k) * J.stride];
+      }
+#pragma unroll
+      for (int k = 0; k < 7; ++k)
+        if (b + k < J.nb) v[k] += p[(long long)(b + k) * J.stride];
+      buf[J.base + e] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+    }
+    return;
+  }
+  // work items: a chunk in kSumChunk / (256 per) parts of 256 per elements,
+  // `per` (1, 2, 4 or 8) elements per thread, 256 apart
+  const int per = a.per;
+  const int parts = kSumChunk / (256 * per);
+  const long long nitems = a.total / kSumChunk * parts;
+  for (long long item = (long long)blockIdx.x - a.rec_blocks; item < nitems; item += nb) {
+    const long long ch = item / parts;
+    const int part = (int)(item - ch * parts);
     const long long gg = a.first + ch * kSumChunk;   // first element of the chunk among all sum jobs
     int lo = 0, hi = a.njobs - 1;
     while (lo < hi) {
@@ -597,7 +632,7 @@ __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
       if ((cached ? sfirst[mid] : a.jobs[mid].first) <= gg) lo = mid; else hi = mid - 1;
     }
     const SumJob J = a.jobs[lo];
-    const long long e0 = gg - J.first;
+    const long long e0 = gg - J.first + (long long)part * 256 * per;
     T* p = buf + J.base + e0;
     constexpr int kPer = kSumChunk / 256;
     bool ok[kPer];
@@ -605,7 +640,7 @@ __global__ void __launch_bounds__(256) post_modal_kernel(PostModalArgs<T> a) {
 #pragma unroll
     for (int i = 0; i < kPer; ++i) {
       const int idx = (int)threadIdx.x + 256 * i;
-      ok[i] = e0 + idx < J.count;
+      ok[i] = i < per && e0 + idx < J.count;
       v[i] = ok[i] ? p[idx] : (T)0;
     }
 #pragma unroll 2

@@ -116,3 +116,29 @@ def test_modal_kx_reduce_scatter(G):
             q = li // o1
             assert q == 4 * bool(li & o4) + 2 * bool(li & o2) + bool(li & o1)
             assert h1[li] == total[q]
+
+
+@pytest.mark.parametrize("per", [1, 2, 4, 8])
+def test_partial_sum_items_cover_every_element_once(per):
+    """post_modal_kernel's partial sums (ard_kernels.cuh): jobs start on
+    kSumChunk boundaries of the index space; work item -> (chunk, part),
+    thread tid takes elements e0 + tid + 256 i for i < per.  Every element of
+    every job is summed exactly once, for each elements-per-thread choice."""
+    chunk = 2048
+    counts = [6, 2047, 2048, 2049, 9600, 5000, 1, 4096]
+    first, t = [], 0
+    for c in counts:
+        first.append(t)
+        t += (c + chunk - 1) // chunk * chunk
+    parts = chunk // (256 * per)
+    seen = [np.zeros(c, int) for c in counts]
+    for item in range(t // chunk * parts):
+        ch, part = divmod(item, parts)
+        gg = ch * chunk
+        lo = max(i for i in range(len(first)) if first[i] <= gg)
+        e0 = gg - first[lo] + part * 256 * per
+        idx = np.arange(256)[:, None] + 256 * np.arange(per)[None, :]
+        e = (e0 + idx).ravel()
+        e = e[e < counts[lo]]
+        np.add.at(seen[lo], e, 1)
+    assert all((s == 1).all() for s in seen)
