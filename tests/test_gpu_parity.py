@@ -2,7 +2,7 @@
 (golden fixtures made by the reference build) and the oracle.
 
 Tolerances: FP32 recorder signals within 1e-4 relative L2 of the reference
-(the spec bar); the FP64 GPU oracle within 1e-10 of the FP64 C oracle
+(the FP32 accuracy bar); the FP64 GPU oracle within 1e-10 of the FP64 C oracle
 (same algorithm, different summation order)."""
 import numpy as np
 import pytest
@@ -53,7 +53,7 @@ def test_fields_match_oracle(name):
     ref.step(sc["steps"])
     _, sim = gpu_run(sc, g["sources"])
     wants = [ref.field(i)[0] for i in range(len(flat["partitions"]))]
-    scale = max(np.abs(w).max() for w in wants)   # near-silent PML slabs are judged on the scene's scale
+    scale = max(np.abs(w).max() for w in wants)   # near-silent PML slabs are measured against the scene's scale
     for i, want in enumerate(wants):
         got = sim.field(i)
         assert np.abs(got - want).max() / scale < 1e-4, i
